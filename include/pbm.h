@@ -1,0 +1,207 @@
+/*
+ * pbm.h -- C ABI of the GB300 page and buffer manager (libpbm.so).
+ *
+ * Plain pointers and sizes only.  Pointers named d_* are device pointers
+ * (cudaMalloc'd by the caller), h_* are host pointers, `stream` is a
+ * cudaStream_t (NULL = legacy default stream).  Every function returns
+ * PBM_OK (0) or a negative status; nothing calls exit() or traps.
+ *
+ * Each entry point cites the reference interface it replaces.  The
+ * reference keeps one implicit pool per translation unit in __device__
+ * globals (source/Paging.cuh:37-42, RandomWalkBasic_BM.cuh:28-31); here a
+ * pool is an explicit handle, and the reference-named host functions in
+ * pbm/ *.cuh bind a per-TU default pool to it.
+ */
+#ifndef PBM_H
+#define PBM_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ---- */
+#define PBM_OK               0
+#define PBM_ERR_INVALID     -1   /* bad argument */
+#define PBM_ERR_CUDA        -2   /* a CUDA call failed */
+#define PBM_ERR_NOMEM       -3   /* device or host allocation failed */
+#define PBM_ERR_EXHAUSTED   -4   /* some requests found no page within their step bound */
+#define PBM_ERR_TIMEOUT     -5   /* a bounded device wait gave up */
+#define PBM_ERR_UNSUPPORTED -6   /* option not available for this strategy */
+#define PBM_ERR_CORRUPT     -7   /* an invariant check failed */
+
+/* ---- allocation strategies (reference names in brackets) ---- */
+#define PBM_RANDOM_WALK        0 /* page probe   [getPage, RandomWalkBasic.cuh:54; getPageRandomWalk, parallelPage.cu:152] */
+#define PBM_RANDOM_WALK_BM     1 /* word probe   [getPage, RandomWalkBasic_BM.cuh:60; getPageRandomWalk_BM, parallelPage.cu:1066] */
+#define PBM_COLLAB_RW_BM       2 /* warp collab  [getPage, CollabRW_BM.cuh:114; getPageCollabRW(_BM), parallelPage.cu:643,830] */
+#define PBM_CLUSTERED_RW_BM    3 /* clustered    [getPage, CRW_BM.cuh:75; getPageClusteredRandomWalk(_BM), parallelPage.cu:243,1203] */
+#define PBM_LINKED_LIST        4 /* FIFO list    [getPageLinkedList, parallelPage.cu:342] */
+#define PBM_SINGLE_CLOCK       5 /* shared arm   [getPageSingleClock, parallelPage.cu:491] */
+#define PBM_DIST_CLOCK         6 /* slot arms    [getPageDistClock, parallelPage.cu:571] */
+#define PBM_N_STRATEGIES       7
+
+/* ---- batch operations ---- */
+#define PBM_OP_ALLOC   0   /* ids[i] <- new page (or -1) */
+#define PBM_OP_FREE    1   /* free ids[i] (ids < 0 are skipped) */
+#define PBM_OP_SWAP    2   /* allocate a new page, free ids[i], ids[i] <- new page
+                              (on failure ids[i] keeps its page) */
+
+/* ---- launch forms ---- */
+#define PBM_LAUNCH_PLAIN       0   /* one kernel launch per group */
+#define PBM_LAUNCH_PERSISTENT  1   /* one persistent kernel over all groups */
+
+/* Pool flags */
+#define PBM_POOL_MATERIALIZE   1u  /* also reserve n_pages*page_size bytes of page memory */
+
+typedef struct pbm_pool pbm_pool;
+
+typedef struct {
+    uint64_t n_pages;      /* T, 1 .. 2^31-1 */
+    uint32_t page_size;    /* bytes per page */
+    uint32_t flags;        /* PBM_POOL_* */
+    uint32_t max_slots;    /* per-slot walker state (clustered cursors, clock arms); 0 = 1<<22 */
+    uint32_t reserved;
+} pbm_pool_config;
+
+typedef struct {
+    int32_t  strategy;      /* PBM_RANDOM_WALK ... */
+    int32_t  word_bits;     /* 32 or 64 (word-probe and collaborative walks) */
+    int32_t  collab_width;  /* 8, 16 or 32 lanes per collaborating group */
+    uint32_t stride;        /* words between neighbouring lanes of a collaborating group (>=1) */
+    uint32_t max_steps;     /* bound on random jumps per request (0 = 4096) */
+    int32_t  block_size;    /* threads per block (0 = 256) */
+    int32_t  blocks_per_sm; /* persistent form: resident blocks per SM (0 = occupancy limit) */
+    int32_t  free_merge;    /* 1 = merge frees of one word within a warp */
+} pbm_walk_config;
+
+/* One caller's group in a batch.  Requests of the batch are numbered in
+ * group order; request q uses LCG seed request_seed(seed, q). */
+typedef struct {
+    int32_t  op;           /* PBM_OP_* */
+    uint32_t count;        /* requests in this group */
+    uint64_t offset;       /* first slot of the group in the id arena (wraps at arena_len) */
+} pbm_group;
+
+typedef struct {
+    uint64_t successes;    /* pages obtained */
+    uint64_t failures;     /* requests that hit their step bound */
+    uint64_t steps;        /* sum of per-request steps */
+    uint64_t frees;        /* pages released */
+} pbm_stats;
+
+typedef struct {
+    int64_t n_ok, n_failed, n_out_of_range, n_duplicates, n_not_marked;
+    int64_t used_pages;    /* popcount of the bitmap after the check */
+} pbm_check_result;
+
+/* ---------------- pool ---------------- */
+
+/* initMemoryManagement(nGB, pageSize) [RandomWalkBasic.cuh:39-48, Paging.cuh:59-85],
+ * initPages*() [parallelPage.cu:53-71,111-146].  One contiguous reservation
+ * instead of 1 GB groups; the bitmap starts all-free. */
+int pbm_pool_create(const pbm_pool_config *cfg, pbm_pool **out);
+/* (no reference counterpart: the reference never frees its pool) */
+int pbm_pool_destroy(pbm_pool *pool);
+/* Device addresses and sizes of the pool (bitmap, page memory). */
+int pbm_pool_info(const pbm_pool *pool, uint64_t *n_pages, uint32_t *page_size,
+                  void **d_bitmap, size_t *bitmap_bytes, void **d_base);
+/* resetMemoryManager() [RandomWalkBasic.cuh:86-88]; resetBuffer*() [parallelPage.cu:185-193 ...].
+ * Frees every page and resets clock arms, cursors and the free list. */
+int pbm_pool_reset(pbm_pool *pool, void *stream);
+/* prefillBuffer(freePercentage) [RandomWalkBasic.cuh:121-131]: instead of an
+ * allocation run, sets each page held i.i.d. with probability `occupancy`
+ * from a counter-based hash of (seed, page). */
+int pbm_pool_prefill_bernoulli(pbm_pool *pool, double occupancy, uint64_t seed, void *stream);
+/* getFreePagePercentage() [RandomWalkBasic_BM.cuh:117-145], printNumPagesLeft*():
+ * number of held pages (popcount of the bitmap); synchronises `stream`. */
+int pbm_pool_used(pbm_pool *pool, uint64_t *h_used, void *stream);
+/* Snapshot / restore of the bitmap (bytes = bitmap_bytes); synchronous. */
+int pbm_pool_read_bitmap(pbm_pool *pool, void *h_dst, size_t bytes, void *stream);
+int pbm_pool_write_bitmap(pbm_pool *pool, const void *h_src, size_t bytes, void *stream);
+/* Accumulated device statistics since create/reset (synchronises `stream`). */
+int pbm_pool_stats(pbm_pool *pool, pbm_stats *h_out, void *stream);
+
+/* ---------------- page allocation ---------------- */
+
+/* n requests, one page each: d_ids[i] <- page or -1, d_steps[i] <- steps
+ * (d_steps may be NULL).  [getPage*(int*) from every strategy, launched as
+ * the reference's drivers do, e.g. get1page_kernel, unitTest1.cu:22-30] */
+int pbm_alloc(pbm_pool *pool, const pbm_walk_config *cfg, uint32_t n, uint32_t seed,
+              int32_t *d_ids, int32_t *d_steps, void *stream);
+/* Same requests processed in order by one thread (one warp for the
+ * collaborative walk): a deterministic replay. */
+int pbm_alloc_serial(pbm_pool *pool, const pbm_walk_config *cfg, uint32_t n, uint32_t seed,
+                     int32_t *d_ids, int32_t *d_steps, void *stream);
+/* freePage*(pageID) [RandomWalkBasic.cuh:82-84, RandomWalkBasic_BM.cuh:98-102,
+ * parallelPage.cu:180,265,...]: ids < 0 are skipped. */
+int pbm_free(pbm_pool *pool, const pbm_walk_config *cfg, uint32_t n, const int32_t *d_ids,
+             void *stream);
+/* Contiguous runs: d_npages[i] pages (1..32) inside one bitmap word.
+ * [getXPageRandomWalk_BM, parallelPage.cu:1104-1142; getNPage, RWMalloc.cuh:203-248] */
+int pbm_alloc_runs(pbm_pool *pool, uint32_t n, const int32_t *d_npages, uint32_t seed,
+                   uint32_t max_steps, int32_t *d_ids, int32_t *d_steps, void *stream);
+int pbm_alloc_runs_serial(pbm_pool *pool, uint32_t n, const int32_t *d_npages, uint32_t seed,
+                          uint32_t max_steps, int32_t *d_ids, int32_t *d_steps, void *stream);
+/* [releasePages, CollabRW_BM.cuh:61-71; freeRW, RWMalloc.cuh:329-334] */
+int pbm_free_runs(pbm_pool *pool, uint32_t n, const int32_t *d_ids, const int32_t *d_npages,
+                  void *stream);
+
+/* The page-pool workload of the reference's drivers: each of n requests
+ * claims one page (page-probe walk), writes its request index into the
+ * first payload_bytes of the page and frees it again unless `hold`.
+ * Needs a pool created with PBM_POOL_MATERIALIZE.
+ * [get1page_kernel + freePage_kernel, unitTest1.5.cu:127-150; getPagePtr,
+ * RandomWalkBasic.cuh:76-79] */
+int pbm_claim_write_free(pbm_pool *pool, uint32_t n, uint32_t seed, uint32_t payload_bytes, int hold,
+                         uint32_t max_steps, int32_t *d_ids, int32_t *d_steps, void *stream);
+/* Copies the first bytes_per_page bytes of each listed page into d_out
+ * (n * bytes_per_page bytes; ids < 0 give zeros).  [pageAddress, Paging.cuh:30-38] */
+int pbm_gather_pages(pbm_pool *pool, const int32_t *d_ids, uint32_t n, uint32_t bytes_per_page,
+                     int32_t *d_out, void *stream);
+
+/* ---------------- batches ---------------- */
+
+/* Runs the groups of one batch.  d_groups: device array of n_groups
+ * descriptors; h_groups: the same descriptors in host memory (needed by the
+ * plain form, which launches one kernel per group; may be NULL for the
+ * persistent form).  d_arena: id arena of arena_len slots.  The persistent
+ * form is a single launch and can be captured in a CUDA graph. */
+int pbm_batch_launch(pbm_pool *pool, const pbm_walk_config *cfg, const pbm_group *d_groups,
+                     const pbm_group *h_groups, uint32_t n_groups, int32_t *d_arena,
+                     uint64_t arena_len, uint32_t seed, int32_t *d_steps, int mode, void *stream);
+
+/* Graph-replayed persistent batch.  The descriptors of step k are read from
+ * d_groups + k*n_groups with seed seed0 + k, where k is a device-resident
+ * counter that each replay advances; replay with pbm_graph_replay. */
+typedef struct pbm_graph pbm_graph;
+int pbm_batch_graph_create(pbm_pool *pool, const pbm_walk_config *cfg, const pbm_group *d_groups,
+                           uint32_t n_groups, uint32_t n_steps, int32_t *d_arena,
+                           uint64_t arena_len, uint32_t seed0, void *stream, pbm_graph **out);
+int pbm_graph_replay(pbm_graph *g, void *stream);
+int pbm_graph_set_step(pbm_graph *g, uint32_t step, void *stream);
+int pbm_graph_destroy(pbm_graph *g);
+
+/* ---------------- checks and measurement ---------------- */
+
+/* Invariants of an allocation result: ids in range, no page handed to two
+ * requesters, every returned page marked held; plus the pool's popcount. */
+int pbm_check_ids(pbm_pool *pool, const int32_t *d_ids, uint32_t n, pbm_check_result *h_out,
+                  void *stream);
+
+/* Uncontended atomicOr ceiling: `threads` threads each issue `iters`
+ * returning atomicOr operations on distinct words of a `words`-word buffer
+ * spread over the L2 slices.  h_ops_per_s <- RMW/s measured with CUDA events. */
+int pbm_atomic_ceiling(uint32_t words, uint32_t threads, uint32_t iters, int returning,
+                       double *h_ops_per_s, double *h_ms);
+
+/* Library identity and the number of kernels this library has launched. */
+const char *pbm_version(void);
+uint64_t pbm_kernel_launches(void);
+int pbm_device_sm_count(int *h_sms);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* PBM_H */

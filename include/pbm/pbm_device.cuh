@@ -1,0 +1,446 @@
+// pbm_device.cuh -- device-side core of the GB300 page manager.
+//
+// Everything a kernel needs to allocate and free pages of a pool from any
+// thread: the pool descriptor, the reference's LCG, the index mapping, and
+// the walks (per-thread page probe, per-thread word probe, warp-collaborative
+// walk, clustered walk, clock sweeps, contiguous runs) plus frees.
+//
+// The same inline routines run inside this library's batch kernels and in a
+// caller's own kernels through the drop-in headers (RandomWalkBasic.cuh,
+// RandomWalkBasic_BM.cuh, CollabRW_BM.cuh, CRW_BM.cuh, RWMalloc.cuh,
+// parallelPage.cuh).
+//
+// Bitmap layout: bit b of 32-bit word w <-> page 32*w + b; bit set = held.
+// The 64-bit view reads the same bytes (page 64*w + b), so the storage is
+// padded to an even number of 32-bit words and every bit past the last page
+// is kept set.  All walks are bounded: after max_steps random jumps a
+// request returns -1 instead of trapping or spinning.
+#pragma once
+#include <cstdint>
+
+namespace pbm {
+
+// Pool descriptor, passed by value (or read from a __device__ global by the
+// drop-in API).  32 bytes.
+struct PoolView {
+    uint32_t* words;      // bitmap, n_words32 (even) 32-bit words
+    char*     base;       // page memory (pageAddress), may be null
+    uint32_t  n_pages;    // T
+    uint32_t  n_words32;  // ceil(T/32)
+    uint32_t  n_words64;  // ceil(T/64)
+    uint32_t  page_size;  // bytes
+};
+
+constexpr uint32_t kFull32 = 0xffffffffu;
+constexpr uint64_t kFull64 = 0xffffffffffffffffull;
+
+// ---------------------------------------------------------------------------
+// RNG
+// ---------------------------------------------------------------------------
+
+// source/RNG_LCG.cuh:9-12: (1103515245*x + 12345) % (1<<31) in signed 64-bit
+// with C truncation, cast to int.  The remainder by 2^31 is a mask of the
+// magnitude, so no 64-bit division is issued.
+__host__ __device__ __forceinline__ int32_t lcg(int32_t x) {
+    long long v = 1103515245LL * (long long)x + 12345LL;
+    long long r = v >= 0 ? (v & 0x7fffffffLL) : -((-v) & 0x7fffffffLL);
+    return (int32_t)r;
+}
+
+// Index in [0, n) from the LCG state's 31 bits by multiply-high.  The
+// reference reduces with `(unsigned)x % n`; for power-of-two n that keeps
+// only the LCG's low bits, whose short periods make threads with equal low
+// seed bits walk identical sequences.  The high bits do not have that flaw.
+__host__ __device__ __forceinline__ uint32_t idx_hi(int32_t x, uint32_t n) {
+    return (uint32_t)((((unsigned long long)((uint32_t)x & 0x7fffffffu)) * n) >> 31);
+}
+
+// Per-request seed: murmur3 fmix32 of (stream seed, request index), 31 bits.
+__host__ __device__ __forceinline__ int32_t request_seed(uint32_t S, uint32_t r) {
+    uint32_t h = r * 0x9E3779B1u + S * 0x85EBCA77u + 0x165667B1u;
+    h ^= h >> 16; h *= 0x85EBCA6Bu;
+    h ^= h >> 13; h *= 0xC2B2AE35u;
+    h ^= h >> 16;
+    return (int32_t)(h & 0x7fffffffu);
+}
+
+// splitmix64 output function on a Weyl counter (Bernoulli prefill).
+__host__ __device__ __forceinline__ uint64_t hash64(uint64_t seed, uint64_t ctr) {
+    uint64_t z = seed * 0xD1B54A32D192ED03ull + (ctr + 1ull) * 0x9E3779B97F4A7C15ull;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+
+#ifdef __CUDACC__
+
+// ---------------------------------------------------------------------------
+// Word access
+// ---------------------------------------------------------------------------
+
+// Bitmap loads bypass L1 (it is not coherent with the L2 atomics); a stale
+// value would only waste a probe, the atomic stays authoritative.
+__device__ __forceinline__ uint32_t load_word(const uint32_t* p) { return __ldcg(p); }
+__device__ __forceinline__ uint64_t load_word(const uint64_t* p) {
+    return (uint64_t)__ldcg(reinterpret_cast<const unsigned long long*>(p));
+}
+__device__ __forceinline__ uint32_t atomic_or(uint32_t* p, uint32_t m) { return atomicOr(p, m); }
+__device__ __forceinline__ uint64_t atomic_or(uint64_t* p, uint64_t m) {
+    return (uint64_t)atomicOr(reinterpret_cast<unsigned long long*>(p), (unsigned long long)m);
+}
+__device__ __forceinline__ void atomic_and_noret(uint32_t* p, uint32_t m) { atomicAnd(p, m); }
+__device__ __forceinline__ void atomic_and_noret(uint64_t* p, uint64_t m) {
+    atomicAnd(reinterpret_cast<unsigned long long*>(p), (unsigned long long)m);
+}
+__device__ __forceinline__ int popc_w(uint32_t x) { return __popc(x); }
+__device__ __forceinline__ int popc_w(uint64_t x) { return __popcll(x); }
+__device__ __forceinline__ int ctz_w(uint32_t x) { return __ffs((int)x) - 1; }
+__device__ __forceinline__ int ctz_w(uint64_t x) { return __ffsll((long long)x) - 1; }
+
+// Lowest k set bits of m (0 <= k <= popc(m)).
+__device__ __forceinline__ uint32_t low_bits(uint32_t m, int k) {
+    if (k <= 0) return 0u;
+    if (k >= __popc(m)) return m;
+    uint32_t pos = __fns(m, 0u, k + 1);       // position of the (k+1)-th set bit
+    return m & ((1u << pos) - 1u);
+}
+__device__ __forceinline__ uint64_t low_bits(uint64_t m, int k) {
+    if (k <= 0) return 0ull;
+    uint32_t lo = (uint32_t)m, hi = (uint32_t)(m >> 32);
+    int clo = __popc(lo);
+    if (k <= clo) return (uint64_t)low_bits(lo, k);
+    return (uint64_t)lo | ((uint64_t)low_bits(hi, k - clo) << 32);
+}
+
+template <typename Word> struct WordTraits;
+template <> struct WordTraits<uint32_t> {
+    static constexpr int kBits = 32;
+    static constexpr int kShift = 5;
+    __device__ static uint32_t full() { return kFull32; }
+    __device__ static uint32_t count(const PoolView& v) { return v.n_words32; }
+};
+template <> struct WordTraits<uint64_t> {
+    static constexpr int kBits = 64;
+    static constexpr int kShift = 6;
+    __device__ static uint64_t full() { return kFull64; }
+    __device__ static uint32_t count(const PoolView& v) { return v.n_words64; }
+};
+
+// ---------------------------------------------------------------------------
+// Per-thread page-probe walk (RandomWalkBasic semantics, on the bitmap):
+// probe a random page; if its bit is clear try to set it; steps = probes.
+// source/RandomWalkBasic.cuh:54-74
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ int32_t walk_page(const PoolView& v, int32_t seed0,
+                                             uint32_t max_steps, int32_t* steps_out) {
+    int32_t x = seed0;
+    uint32_t s = 0;
+    while (s < max_steps) {
+        ++s;
+        x = lcg(x);
+        uint32_t p = idx_hi(x, v.n_pages);
+        uint32_t* wp = v.words + (p >> 5);
+        uint32_t bit = 1u << (p & 31u);
+        if (load_word(wp) & bit) continue;
+        uint32_t old = atomicOr(wp, bit);
+        if (!(old & bit)) {
+            if (steps_out) *steps_out = (int32_t)s;
+            return (int32_t)p;
+        }
+    }
+    if (steps_out) *steps_out = (int32_t)s;
+    return -1;
+}
+
+// ---------------------------------------------------------------------------
+// Per-thread word-probe walk (RandomWalkBasic_BM semantics): jump to a random
+// word, claim its lowest clear bit; on a lost race retry in the same word;
+// steps = jumps.  source/RandomWalkBasic_BM.cuh:60-89
+// ---------------------------------------------------------------------------
+template <typename Word>
+__device__ __forceinline__ int32_t walk_word(const PoolView& v, int32_t seed0,
+                                             uint32_t max_steps, int32_t* steps_out) {
+    using T = WordTraits<Word>;
+    Word* words = reinterpret_cast<Word*>(v.words);
+    const uint32_t L = T::count(v);
+    int32_t x = seed0;
+    uint32_t s = 0;
+    while (s < max_steps) {
+        ++s;
+        x = lcg(x);
+        uint32_t w = idx_hi(x, L);
+        Word val = load_word(words + w);
+        while (val != T::full()) {
+            int b = ctz_w((Word)~val);
+            Word bit = (Word)1 << b;
+            Word old = atomic_or(words + w, bit);
+            if (!(old & bit)) {
+                if (steps_out) *steps_out = (int32_t)s;
+                return (int32_t)(((uint32_t)w << T::kShift) + (uint32_t)b);
+            }
+            val = old | bit;
+        }
+    }
+    if (steps_out) *steps_out = (int32_t)s;
+    return -1;
+}
+
+// ---------------------------------------------------------------------------
+// Warp-collaborative walk (CollabRW_BM, source/CollabRW_BM.cuh:114-160,
+// restated lock-free).  A group of W lanes (W = 8, 16 or 32, aligned within
+// the warp) shares one LCG stream.  Per iteration lane i reads word
+// (base + i*stride) mod L with one coalesced load when stride == 1; the
+// group claims exactly as many clear bits as it still needs -- lowest lanes
+// and lowest bits first, one atomicOr per word -- and hands the bits it
+// gained to the needing lanes in lane order.  Nothing is over-claimed, so
+// nothing is written back.  Lanes whose words coincide (only possible when
+// W*stride > L) are de-duplicated with __match_any_sync.
+//
+// Every lane of the group must call this converged; `need` says whether the
+// lane requests a page.  All lanes of the group report the same step count
+// (iterations of the group), as in the reference.  `slots` is a per-group
+// scratch of W ints in shared memory.
+// ---------------------------------------------------------------------------
+template <int W, typename Word>
+__device__ __forceinline__ int32_t walk_collab(const PoolView& v, bool need, int32_t group_seed,
+                                               uint32_t lane_off /* (lane_in_group*stride) % L */,
+                                               bool dedupe, uint32_t max_steps,
+                                               volatile int32_t* slots, int32_t* steps_out) {
+    using T = WordTraits<Word>;
+    Word* words = reinterpret_cast<Word*>(v.words);
+    const uint32_t L = T::count(v);
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t gl = lane & (uint32_t)(W - 1);                    // lane in group
+    const uint32_t gmask = (W == 32) ? kFull32 : (((1u << W) - 1u) << (lane & ~(uint32_t)(W - 1)));
+    const uint32_t lt = (1u << lane) - 1u;                           // lanes below me
+    int32_t id = -1;
+    int32_t x = group_seed;
+    uint32_t needm = __ballot_sync(gmask, need);
+    uint32_t s = 0;
+    while (needm && s < max_steps) {
+        ++s;
+        x = lcg(x);
+        uint32_t w = idx_hi(x, L) + lane_off;
+        if (w >= L) w -= L;
+        Word val = load_word(words + w);
+        if (dedupe) {
+            uint32_t peers = __match_any_sync(gmask, w);
+            if ((peers & lt) != 0u) val = T::full();               // a lower lane reads this word
+        }
+        Word fr = (Word)~val;
+        int cnt = popc_w(fr);
+        // inclusive scan of cnt over the group
+        int incl = cnt;
+#pragma unroll
+        for (int d = 1; d < W; d <<= 1) {
+            int y = __shfl_up_sync(gmask, incl, d, W);
+            if ((int)gl >= d) incl += y;
+        }
+        int n = __popc(needm);
+        int pre = incl - cnt;
+        Word m = low_bits(fr, n - pre);
+        Word got = 0;
+        if (m) {
+            Word old = atomic_or(words + w, m);
+            got = m & (Word)~old;
+        }
+        int g = popc_w(got);
+        int gincl = g;
+#pragma unroll
+        for (int d = 1; d < W; d <<= 1) {
+            int y = __shfl_up_sync(gmask, gincl, d, W);
+            if ((int)gl >= d) gincl += y;
+        }
+        int G = __shfl_sync(gmask, gincl, W - 1, W);
+        int pos = gincl - g;
+        while (got) {
+            int b = ctz_w(got);
+            got &= got - (Word)1;
+            slots[pos++] = (int32_t)(((uint32_t)w << T::kShift) + (uint32_t)b);
+        }
+        __syncwarp(gmask);
+        if (id < 0 && need) {
+            int rank = __popc(needm & lt);
+            if (rank < G) id = slots[rank];
+        }
+        __syncwarp(gmask);
+        needm = __ballot_sync(gmask, need && id < 0);
+    }
+    if (steps_out) *steps_out = (int32_t)s;
+    return id;
+}
+
+// ---------------------------------------------------------------------------
+// Clustered walk (CRW_BM, source/CRW_BM.cuh:75-142): resume at the word of
+// this slot's last page (the next word once the last page was the word's
+// top bit) and claim its lowest clear bit; otherwise random word-probe
+// jumps.  steps = claim attempts (the reference does not count jumps).
+// `cursor` = last page of the slot or -1; updated on success.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ int32_t walk_crw(const PoolView& v, int32_t* cursor, int32_t seed0,
+                                            uint32_t max_steps, int32_t* steps_out) {
+    const uint32_t L = v.n_words32;
+    int32_t s = 0;
+    int32_t last = *cursor;
+    if (last >= 0) {
+        uint32_t w = (uint32_t)last >> 5;
+        if (((uint32_t)last & 31u) == 31u) { w += 1u; if (w == L) w = 0; }
+        uint32_t val = load_word(v.words + w);
+        while (val != kFull32) {
+            ++s;
+            int b = __ffs((int)~val) - 1;
+            uint32_t bit = 1u << b;
+            uint32_t old = atomicOr(v.words + w, bit);
+            if (!(old & bit)) {
+                *cursor = (int32_t)(w * 32u + (uint32_t)b);
+                if (steps_out) *steps_out = s;
+                return *cursor;
+            }
+            val = old | bit;
+        }
+    }
+    int32_t x = seed0;
+    for (uint32_t j = 0; j < max_steps; ++j) {
+        x = lcg(x);
+        uint32_t w = idx_hi(x, L);
+        uint32_t val = load_word(v.words + w);
+        while (val != kFull32) {
+            ++s;
+            int b = __ffs((int)~val) - 1;
+            uint32_t bit = 1u << b;
+            uint32_t old = atomicOr(v.words + w, bit);
+            if (!(old & bit)) {
+                *cursor = (int32_t)(w * 32u + (uint32_t)b);
+                if (steps_out) *steps_out = s;
+                return *cursor;
+            }
+            val = old | bit;
+        }
+    }
+    if (steps_out) *steps_out = s;
+    return -1;
+}
+
+// ---------------------------------------------------------------------------
+// Clock sweeps.  Single clock: one shared arm, atomicAdd then test-and-set
+// (parallelPage.cu:491-509 checks and then exchanges without looking at the
+// old value; here the claim is the atomicOr's old bit).  Distributed clock:
+// a private arm per slot, linear probe (parallelPage.cu:571-592).
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ int32_t sweep_single(const PoolView& v, unsigned long long* arm,
+                                                uint32_t max_steps, int32_t* steps_out) {
+    uint32_t s = 0;
+    while (s < max_steps) {
+        ++s;
+        unsigned long long a = atomicAdd(arm, 1ull);
+        uint32_t p = (uint32_t)(a % v.n_pages);
+        uint32_t* wp = v.words + (p >> 5);
+        uint32_t bit = 1u << (p & 31u);
+        if (load_word(wp) & bit) continue;
+        if (!(atomicOr(wp, bit) & bit)) {
+            if (steps_out) *steps_out = (int32_t)s;
+            return (int32_t)p;
+        }
+    }
+    if (steps_out) *steps_out = (int32_t)s;
+    return -1;
+}
+
+__device__ __forceinline__ int32_t sweep_dist(const PoolView& v, uint32_t* arm,
+                                              uint32_t max_steps, int32_t* steps_out) {
+    uint32_t s = 0, a = *arm;
+    int32_t out = -1;
+    while (s < max_steps) {
+        ++s;
+        uint32_t p = a >= v.n_pages ? a - v.n_pages : a;
+        a = p + 1u;
+        uint32_t* wp = v.words + (p >> 5);
+        uint32_t bit = 1u << (p & 31u);
+        if (load_word(wp) & bit) continue;
+        if (!(atomicOr(wp, bit) & bit)) { out = (int32_t)p; break; }
+    }
+    *arm = a;
+    if (steps_out) *steps_out = (int32_t)s;
+    return out;
+}
+
+// ---------------------------------------------------------------------------
+// Contiguous run of n pages (1..32) inside one 32-bit word, word-probe walk,
+// lowest fitting start, claimed with compare-and-swap so a run is either
+// taken whole or not at all (parallelPage.cu:1104-1142 sets the bits with
+// atomicOr and reverts the wrong ones on a collision; RWMalloc.cuh:203-248).
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t run_starts(uint32_t f, uint32_t n) {
+    uint32_t r = f, len = 1;
+    while (len < n) {
+        uint32_t sh = len < n - len ? len : n - len;
+        r &= r >> sh;
+        len += sh;
+    }
+    return r;
+}
+
+__device__ __forceinline__ int32_t walk_run(const PoolView& v, uint32_t n, int32_t seed0,
+                                            uint32_t max_steps, int32_t* steps_out) {
+    const uint32_t L = v.n_words32;
+    int32_t x = seed0;
+    uint32_t s = 0;
+    while (s < max_steps) {
+        ++s;
+        x = lcg(x);
+        uint32_t w = idx_hi(x, L);
+        uint32_t val = load_word(v.words + w);
+        for (int tries = 0; tries < 64; ++tries) {
+            uint32_t r = run_starts(~val, n);
+            if (!r) break;
+            uint32_t st = (uint32_t)(__ffs((int)r) - 1);
+            uint32_t m = (n >= 32u ? kFull32 : ((1u << n) - 1u)) << st;
+            uint32_t old = atomicCAS(v.words + w, val, val | m);
+            if (old == val) {
+                if (steps_out) *steps_out = (int32_t)s;
+                return (int32_t)(w * 32u + st);
+            }
+            val = old;
+        }
+    }
+    if (steps_out) *steps_out = (int32_t)s;
+    return -1;
+}
+
+// ---------------------------------------------------------------------------
+// Frees.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void free_page(const PoolView& v, int32_t id) {
+    atomicAnd(v.words + ((uint32_t)id >> 5), ~(1u << ((uint32_t)id & 31u)));
+}
+
+__device__ __forceinline__ void free_run(const PoolView& v, int32_t id, uint32_t n) {
+    uint32_t st = (uint32_t)id & 31u;
+    uint32_t m = (n >= 32u ? kFull32 : ((1u << n) - 1u)) << st;
+    atomicAnd(v.words + ((uint32_t)id >> 5), ~m);
+}
+
+// Warp-aggregated free: lanes freeing pages of the same word merge their
+// bits (__match_any_sync + __reduce_or_sync) and one lane issues the AND.
+// `active` = lanes calling converged; lanes with id < 0 free nothing.
+__device__ __forceinline__ void free_page_warp(const PoolView& v, uint32_t active, int32_t id) {
+    const uint32_t lane = threadIdx.x & 31u;
+    uint32_t w = id >= 0 ? ((uint32_t)id >> 5) : 0xffffffffu;
+    uint32_t bit = id >= 0 ? (1u << ((uint32_t)id & 31u)) : 0u;
+    uint32_t peers = __match_any_sync(active, w);
+    uint32_t merged = __reduce_or_sync(peers, bit);
+    if (id >= 0 && (__ffs((int)peers) - 1) == (int)lane) atomicAnd(v.words + w, ~merged);
+}
+
+__device__ __forceinline__ void* page_address(const PoolView& v, int32_t id) {
+    return (void*)(v.base + (size_t)(uint32_t)id * v.page_size);
+}
+
+__device__ __forceinline__ int32_t page_id(const PoolView& v, const void* p) {
+    size_t off = (size_t)((const char*)p - v.base);
+    if ((const char*)p < v.base || off >= (size_t)v.n_pages * v.page_size) return -1;
+    return (int32_t)(off / v.page_size);
+}
+
+#endif  // __CUDACC__
+}  // namespace pbm

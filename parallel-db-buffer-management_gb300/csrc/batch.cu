@@ -1,0 +1,435 @@
+// batch.cu -- batched alloc / free / swap requests from many caller groups.
+//
+// Requests of a batch are numbered in group order (q = 0 .. total-1) and
+// request q always uses LCG seed request_seed(seed, q).  Three launch forms
+// run the same requests:
+//   plain       one kernel launch per group (what a caller gets by launching
+//               its own kernel per batch, unitTest1.cu:64 style);
+//   persistent  one kernel over all groups, a grid of (SMs x resident blocks)
+//               warps striding over 32-request chunks; each lane finds its
+//               group by binary search in the groups' prefix sums;
+//   graph       the persistent form captured once in a CUDA graph together
+//               with its prefix kernel and a step-advance kernel, so each
+//               replay reads the next step's descriptors from device memory.
+#include "internal.cuh"
+
+namespace pbm {
+
+enum class BWalk { Page, Word32, Word64, Collab };
+
+struct BatchArgs {
+    PoolView v;
+    const pbm_group* groups;            // base of the descriptor table
+    uint32_t n_groups;
+    const uint32_t* d_step;             // graph form: step counter (may be null)
+    uint32_t seed;
+    int32_t* arena;
+    unsigned long long arena_len;
+    int32_t* steps;                     // parallel to arena, may be null
+    const unsigned long long* prefix;   // persistent: n_groups + 1 exclusive prefix
+    uint32_t max_steps;
+    uint32_t stride;
+    int32_t dedupe;
+    int32_t merge;
+    DevStats* stats;
+    // plain form: the one group this launch serves
+    int32_t op;
+    uint32_t count;
+    unsigned long long offset;
+    unsigned long long q_base;
+};
+
+struct BAcc {
+    unsigned long long ok = 0, fail = 0, steps = 0, frees = 0;
+};
+
+__device__ __forceinline__ void flush_bacc(const BAcc& a, DevStats* st) {
+    __shared__ unsigned long long sh[4];
+    if (threadIdx.x == 0) { sh[0] = sh[1] = sh[2] = sh[3] = 0; }
+    __syncthreads();
+    unsigned long long v0 = a.ok, v1 = a.fail, v2 = a.steps, v3 = a.frees;
+#pragma unroll
+    for (int d = 16; d > 0; d >>= 1) {
+        v0 += __shfl_down_sync(0xffffffffu, v0, d);
+        v1 += __shfl_down_sync(0xffffffffu, v1, d);
+        v2 += __shfl_down_sync(0xffffffffu, v2, d);
+        v3 += __shfl_down_sync(0xffffffffu, v3, d);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        if (v0) atomicAdd(&sh[0], v0);
+        if (v1) atomicAdd(&sh[1], v1);
+        if (v2) atomicAdd(&sh[2], v2);
+        if (v3) atomicAdd(&sh[3], v3);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        if (sh[0]) atomicAdd(&st->successes, sh[0]);
+        if (sh[1]) atomicAdd(&st->failures, sh[1]);
+        if (sh[2]) atomicAdd(&st->steps, sh[2]);
+        if (sh[3]) atomicAdd(&st->frees, sh[3]);
+    }
+}
+
+// One warp-wide round: every lane of the warp calls converged.
+template <BWalk K, int W, typename Word>
+__device__ __forceinline__ void batch_round(const BatchArgs& a, uint32_t seed, bool active, int op,
+                                            unsigned long long q, unsigned long long slot,
+                                            uint32_t lane_off, volatile int32_t* gslots, BAcc& acc) {
+    const bool need = active && (op == PBM_OP_ALLOC || op == PBM_OP_SWAP);
+    int32_t s = 0, id = -1;
+    if constexpr (K == BWalk::Collab) {
+        const uint32_t gl = threadIdx.x & (uint32_t)(W - 1);
+        id = walk_collab<W, Word>(a.v, need, request_seed(seed, (uint32_t)(q - gl)), lane_off,
+                                  a.dedupe != 0, a.max_steps, gslots, &s);
+    } else if (need) {
+        const int32_t seed0 = request_seed(seed, (uint32_t)q);
+        if constexpr (K == BWalk::Page) id = walk_page(a.v, seed0, a.max_steps, &s);
+        else if constexpr (K == BWalk::Word32) id = walk_word<uint32_t>(a.v, seed0, a.max_steps, &s);
+        else id = walk_word<uint64_t>(a.v, seed0, a.max_steps, &s);
+    }
+    int32_t to_free = -1;
+    if (active) {
+        if (op == PBM_OP_ALLOC) {
+            a.arena[slot] = id;
+        } else {
+            int32_t old = a.arena[slot];
+            if (op == PBM_OP_FREE) {
+                to_free = old;
+            } else if (id >= 0) {           // swap
+                a.arena[slot] = id;
+                to_free = old;
+            }
+        }
+        if (to_free >= (int32_t)a.v.n_pages) to_free = -1;
+        if (need) {
+            if (a.steps) a.steps[slot] = s;
+            acc.ok += id >= 0;
+            acc.fail += id < 0;
+            acc.steps += (unsigned long long)s;
+        }
+        acc.frees += to_free >= 0;
+    }
+    if (a.merge) free_page_warp(a.v, 0xffffffffu, to_free);
+    else if (to_free >= 0) free_page(a.v, to_free);
+}
+
+template <BWalk K, int W, typename Word>
+__global__ void __launch_bounds__(256) k_batch_persistent(BatchArgs a) {
+    __shared__ int32_t slots[256];
+    BAcc acc;
+    const uint32_t step = a.d_step ? *a.d_step : 0u;
+    const pbm_group* groups = a.groups + (size_t)step * a.n_groups;
+    const uint32_t seed = a.seed + step;
+    const unsigned long long total = a.prefix[a.n_groups];
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t gl = threadIdx.x & (uint32_t)(W - 1);
+    const uint32_t L = WordTraits<Word>::count(a.v);
+    const uint32_t lane_off = (uint32_t)(((unsigned long long)gl * a.stride) % L);
+    volatile int32_t* gslots = slots + (threadIdx.x & ~(uint32_t)(W - 1));
+    const unsigned long long warp0 = ((unsigned long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const unsigned long long nwarps = ((unsigned long long)gridDim.x * blockDim.x) >> 5;
+    for (unsigned long long chunk = warp0; chunk * 32ull < total; chunk += nwarps) {
+        const unsigned long long q = chunk * 32ull + lane;
+        const bool active = q < total;
+        int op = PBM_OP_ALLOC;
+        unsigned long long slot = 0;
+        if (active) {
+            // upper_bound over prefix[0..n_groups]
+            uint32_t lo = 0, hi = a.n_groups;   // answer g in [0, n_groups)
+            while (lo + 1u < hi) {
+                uint32_t mid = (lo + hi) >> 1;
+                if (a.prefix[mid] <= q) lo = mid; else hi = mid;
+            }
+            const pbm_group gd = groups[lo];
+            op = gd.op;
+            slot = (gd.offset + (q - a.prefix[lo])) % a.arena_len;
+        }
+        batch_round<K, W, Word>(a, seed, active, op, q, slot, lane_off, gslots, acc);
+    }
+    flush_bacc(acc, a.stats);
+}
+
+template <BWalk K, int W, typename Word>
+__global__ void __launch_bounds__(256) k_batch_plain(BatchArgs a) {
+    __shared__ int32_t slots[256];
+    BAcc acc;
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t gl = threadIdx.x & (uint32_t)(W - 1);
+    const uint32_t L = WordTraits<Word>::count(a.v);
+    const uint32_t lane_off = (uint32_t)(((unsigned long long)gl * a.stride) % L);
+    volatile int32_t* gslots = slots + (threadIdx.x & ~(uint32_t)(W - 1));
+    const unsigned long long warp0 = ((unsigned long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const unsigned long long nwarps = ((unsigned long long)gridDim.x * blockDim.x) >> 5;
+    for (unsigned long long chunk = warp0; chunk * 32ull < a.count; chunk += nwarps) {
+        const unsigned long long ql = chunk * 32ull + lane;
+        const bool active = ql < a.count;
+        const unsigned long long slot = (a.offset + ql) % a.arena_len;
+        batch_round<K, W, Word>(a, a.seed, active, a.op, a.q_base + ql, slot, lane_off, gslots, acc);
+    }
+    flush_bacc(acc, a.stats);
+}
+
+// Exclusive prefix of the groups' counts (one block of 1024 threads).
+__global__ void k_batch_prefix(const pbm_group* groups, uint32_t n_groups, const uint32_t* d_step,
+                               unsigned long long* prefix) {
+    __shared__ unsigned long long warp_tot[32];
+    __shared__ unsigned long long carry;
+    const uint32_t step = d_step ? *d_step : 0u;
+    const pbm_group* g = groups + (size_t)step * n_groups;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+    if (threadIdx.x == 0) carry = 0;
+    __syncthreads();
+    for (uint32_t base = 0; base < n_groups; base += blockDim.x) {
+        uint32_t i = base + threadIdx.x;
+        unsigned long long c = i < n_groups ? (unsigned long long)g[i].count : 0ull;
+        unsigned long long incl = c;
+        for (int d = 1; d < 32; d <<= 1) {
+            unsigned long long y = __shfl_up_sync(0xffffffffu, incl, d);
+            if (lane >= d) incl += y;
+        }
+        if (lane == 31) warp_tot[warp] = incl;
+        __syncthreads();
+        if (warp == 0) {
+            unsigned long long t = lane < nwarps ? warp_tot[lane] : 0ull;
+            unsigned long long ti = t;
+            for (int d = 1; d < 32; d <<= 1) {
+                unsigned long long y = __shfl_up_sync(0xffffffffu, ti, d);
+                if (lane >= d) ti += y;
+            }
+            if (lane < nwarps) warp_tot[lane] = ti - t;   // exclusive warp offsets
+        }
+        __syncthreads();
+        unsigned long long excl = carry + warp_tot[warp] + incl - c;
+        if (i < n_groups) prefix[i] = excl;
+        __syncthreads();
+        if (threadIdx.x == blockDim.x - 1) carry = excl + c;
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) prefix[n_groups] = carry;
+}
+
+__global__ void k_step_advance(uint32_t* d_step) {
+    if (threadIdx.x == 0 && blockIdx.x == 0) *d_step += 1u;
+}
+
+}  // namespace pbm
+
+using namespace pbm;
+
+struct pbm_graph {
+    cudaGraph_t graph;
+    cudaGraphExec_t exec;
+    uint32_t* d_step;
+    unsigned long long* d_prefix;
+    unsigned long long launches_per_replay;
+};
+
+namespace {
+
+template <BWalk K, int W, typename Word>
+int launch_batch_kw(const BatchArgs& a, bool persistent, int block, int blocks_per_sm, cudaStream_t s) {
+    if (persistent) {
+        int per_sm = blocks_per_sm;
+        if (per_sm <= 0) {
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch_persistent<K, W, Word>, block, 0);
+            if (per_sm <= 0) per_sm = 1;
+        }
+        k_batch_persistent<K, W, Word><<<sm_count() * per_sm, block, 0, s>>>(a);
+    } else {
+        unsigned long long warps = (a.count + 31ull) / 32ull;
+        unsigned long long grid = (warps * 32ull + (unsigned long long)block - 1ull) / (unsigned long long)block;
+        if (grid < 1) grid = 1;
+        k_batch_plain<K, W, Word><<<(unsigned)grid, block, 0, s>>>(a);
+    }
+    PBM_LAUNCH_CHECK();
+    return PBM_OK;
+}
+
+int launch_batch(const pbm_walk_config* c, const BatchArgs& a, bool persistent, cudaStream_t s) {
+    const int block = c->block_size ? c->block_size : kDefaultBlock;
+    const int bps = c->blocks_per_sm;
+    const bool w64 = c->word_bits == 64;
+    switch (c->strategy) {
+    case PBM_RANDOM_WALK:
+        return launch_batch_kw<BWalk::Page, 32, uint32_t>(a, persistent, block, bps, s);
+    case PBM_RANDOM_WALK_BM:
+        return w64 ? launch_batch_kw<BWalk::Word64, 32, uint64_t>(a, persistent, block, bps, s)
+                   : launch_batch_kw<BWalk::Word32, 32, uint32_t>(a, persistent, block, bps, s);
+    case PBM_COLLAB_RW_BM: {
+        const int W = c->collab_width ? c->collab_width : 32;
+        if (W == 8) return w64 ? launch_batch_kw<BWalk::Collab, 8, uint64_t>(a, persistent, block, bps, s)
+                               : launch_batch_kw<BWalk::Collab, 8, uint32_t>(a, persistent, block, bps, s);
+        if (W == 16) return w64 ? launch_batch_kw<BWalk::Collab, 16, uint64_t>(a, persistent, block, bps, s)
+                                : launch_batch_kw<BWalk::Collab, 16, uint32_t>(a, persistent, block, bps, s);
+        return w64 ? launch_batch_kw<BWalk::Collab, 32, uint64_t>(a, persistent, block, bps, s)
+                   : launch_batch_kw<BWalk::Collab, 32, uint32_t>(a, persistent, block, bps, s);
+    }
+    default:
+        return PBM_ERR_UNSUPPORTED;
+    }
+}
+
+BatchArgs base_args(pbm_pool* p, const pbm_walk_config* c, int32_t* arena, uint64_t arena_len,
+                    uint32_t seed, int32_t* d_steps) {
+    BatchArgs a{};
+    a.v = p->view;
+    a.seed = seed;
+    a.arena = arena;
+    a.arena_len = arena_len;
+    a.steps = d_steps;
+    a.max_steps = c->max_steps ? c->max_steps : kDefaultMaxSteps;
+    a.stride = c->stride ? c->stride : 1u;
+    a.merge = c->free_merge;
+    a.stats = p->d_stats;
+    const int W = c->strategy == PBM_COLLAB_RW_BM ? (c->collab_width ? c->collab_width : 32) : 1;
+    const uint32_t L = c->word_bits == 64 ? p->view.n_words64 : p->view.n_words32;
+    a.dedupe = ((unsigned long long)(W - 1) * a.stride >= L) ? 1 : 0;
+    return a;
+}
+
+int valid_cfg(const pbm_walk_config* c) {
+    if (!c) return PBM_ERR_INVALID;
+    if (c->word_bits != 0 && c->word_bits != 32 && c->word_bits != 64) return PBM_ERR_INVALID;
+    if (c->collab_width != 0 && c->collab_width != 8 && c->collab_width != 16 && c->collab_width != 32)
+        return PBM_ERR_INVALID;
+    if (c->block_size < 0 || c->block_size > 256 || (c->block_size % 32) != 0) return PBM_ERR_INVALID;
+    if (c->strategy != PBM_RANDOM_WALK && c->strategy != PBM_RANDOM_WALK_BM && c->strategy != PBM_COLLAB_RW_BM)
+        return PBM_ERR_UNSUPPORTED;
+    return PBM_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int pbm_batch_launch(pbm_pool* pool, const pbm_walk_config* cfg, const pbm_group* d_groups,
+                     const pbm_group* h_groups, uint32_t n_groups, int32_t* d_arena,
+                     uint64_t arena_len, uint32_t seed, int32_t* d_steps, int mode, void* stream) {
+    if (!pool || !d_arena || arena_len == 0) return PBM_ERR_INVALID;
+    int rc = valid_cfg(cfg);
+    if (rc) return rc;
+    if (n_groups == 0) return PBM_OK;
+    cudaStream_t s = (cudaStream_t)stream;
+    pool->fifo_valid = false;
+    BatchArgs a = base_args(pool, cfg, d_arena, arena_len, seed, d_steps);
+    if (mode == PBM_LAUNCH_PLAIN) {
+        if (!h_groups) return PBM_ERR_INVALID;
+        unsigned long long q = 0;
+        for (uint32_t g = 0; g < n_groups; ++g) {
+            const pbm_group& gd = h_groups[g];
+            if (gd.op < PBM_OP_ALLOC || gd.op > PBM_OP_SWAP) return PBM_ERR_INVALID;
+            if (gd.count == 0) continue;
+            a.op = gd.op;
+            a.count = gd.count;
+            a.offset = gd.offset;
+            a.q_base = q;
+            rc = launch_batch(cfg, a, false, s);
+            if (rc) return rc;
+            q += gd.count;
+        }
+        return PBM_OK;
+    }
+    if (mode != PBM_LAUNCH_PERSISTENT || !d_groups) return PBM_ERR_INVALID;
+    if (pool->prefix_cap < n_groups + 1u) {
+        cudaFree(pool->d_prefix);
+        pool->d_prefix = nullptr;
+        if (cudaMalloc(&pool->d_prefix, sizeof(unsigned long long) * (n_groups + 1u)) != cudaSuccess) {
+            cudaGetLastError();
+            pool->prefix_cap = 0;
+            return PBM_ERR_NOMEM;
+        }
+        pool->prefix_cap = n_groups + 1u;
+    }
+    k_batch_prefix<<<1, 1024, 0, s>>>(d_groups, n_groups, nullptr, pool->d_prefix);
+    PBM_LAUNCH_CHECK();
+    a.groups = d_groups;
+    a.n_groups = n_groups;
+    a.prefix = pool->d_prefix;
+    return launch_batch(cfg, a, true, s);
+}
+
+int pbm_batch_graph_create(pbm_pool* pool, const pbm_walk_config* cfg, const pbm_group* d_groups,
+                           uint32_t n_groups, uint32_t n_steps, int32_t* d_arena, uint64_t arena_len,
+                           uint32_t seed0, void* stream, pbm_graph** out) {
+    if (!pool || !d_groups || !d_arena || !out || n_groups == 0 || n_steps == 0 || arena_len == 0)
+        return PBM_ERR_INVALID;
+    int rc = valid_cfg(cfg);
+    if (rc) return rc;
+    *out = nullptr;
+    cudaStream_t s = (cudaStream_t)stream;
+    pbm_graph* g = new pbm_graph();
+    g->graph = nullptr;
+    g->exec = nullptr;
+    if (cudaMalloc(&g->d_step, sizeof(uint32_t)) != cudaSuccess ||
+        cudaMalloc(&g->d_prefix, sizeof(unsigned long long) * (n_groups + 1u)) != cudaSuccess) {
+        cudaGetLastError();
+        cudaFree(g->d_step);
+        delete g;
+        return PBM_ERR_NOMEM;
+    }
+    PBM_CUDA_TRY(cudaMemsetAsync(g->d_step, 0, sizeof(uint32_t), s));
+    PBM_CUDA_TRY(cudaStreamSynchronize(s));
+    BatchArgs a = base_args(pool, cfg, d_arena, arena_len, seed0, nullptr);
+    a.groups = d_groups;
+    a.n_groups = n_groups;
+    a.prefix = g->d_prefix;
+    a.d_step = g->d_step;
+    const unsigned long long before = g_launches.load();
+    PBM_CUDA_TRY(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+    k_batch_prefix<<<1, 1024, 0, s>>>(d_groups, n_groups, g->d_step, g->d_prefix);
+    count_launch();
+    rc = launch_batch(cfg, a, true, s);
+    k_step_advance<<<1, 32, 0, s>>>(g->d_step);
+    count_launch();
+    cudaGraph_t graph = nullptr;
+    cudaError_t e = cudaStreamEndCapture(s, &graph);
+    if (rc || e != cudaSuccess) {
+        if (graph) cudaGraphDestroy(graph);
+        cudaFree(g->d_step);
+        cudaFree(g->d_prefix);
+        delete g;
+        cudaGetLastError();
+        return rc ? rc : PBM_ERR_CUDA;
+    }
+    g->graph = graph;
+    if (cudaGraphInstantiate(&g->exec, graph, 0) != cudaSuccess) {
+        cudaGraphDestroy(graph);
+        cudaFree(g->d_step);
+        cudaFree(g->d_prefix);
+        delete g;
+        cudaGetLastError();
+        return PBM_ERR_CUDA;
+    }
+    g->launches_per_replay = g_launches.load() - before;
+    // capture does not launch: take the counted launches back
+    g_launches.fetch_sub(g->launches_per_replay);
+    pool->fifo_valid = false;
+    *out = g;
+    return PBM_OK;
+}
+
+int pbm_graph_replay(pbm_graph* g, void* stream) {
+    if (!g || !g->exec) return PBM_ERR_INVALID;
+    PBM_CUDA_TRY(cudaGraphLaunch(g->exec, (cudaStream_t)stream));
+    count_launch(g->launches_per_replay);
+    return PBM_OK;
+}
+
+int pbm_graph_set_step(pbm_graph* g, uint32_t step, void* stream) {
+    if (!g) return PBM_ERR_INVALID;
+    PBM_CUDA_TRY(cudaMemcpyAsync(g->d_step, &step, sizeof(step), cudaMemcpyHostToDevice, (cudaStream_t)stream));
+    PBM_CUDA_TRY(cudaStreamSynchronize((cudaStream_t)stream));
+    return PBM_OK;
+}
+
+int pbm_graph_destroy(pbm_graph* g) {
+    if (!g) return PBM_ERR_INVALID;
+    if (g->exec) cudaGraphExecDestroy(g->exec);
+    if (g->graph) cudaGraphDestroy(g->graph);
+    cudaFree(g->d_step);
+    cudaFree(g->d_prefix);
+    delete g;
+    return PBM_OK;
+}
+
+}  // extern "C"

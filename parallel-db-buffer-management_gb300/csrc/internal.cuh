@@ -1,0 +1,97 @@
+// internal.cuh -- host/device internals shared by the libpbm translation units.
+#pragma once
+#include <cuda_runtime.h>
+#include <atomic>
+#include <cstdint>
+#include <cstdio>
+
+#include "pbm.h"
+#include "pbm/pbm_device.cuh"
+
+namespace pbm {
+
+// Device statistics block (one per pool).
+struct DevStats {
+    unsigned long long successes;
+    unsigned long long failures;
+    unsigned long long steps;
+    unsigned long long frees;
+    unsigned long long timeouts;   // bounded waits that gave up
+    unsigned long long pad[3];
+};
+
+// FIFO free list state (linked-list strategy).
+struct FifoState {
+    unsigned long long head;   // next get ticket
+    unsigned long long tail;   // next put ticket
+    unsigned long long avail;  // free pages, as a signed count in two's complement
+    unsigned long long pad;
+};
+
+// Invariant-check counters.
+struct CheckCounters {
+    unsigned long long ok, failed, out_of_range, duplicates, not_marked, used;
+};
+
+extern std::atomic<unsigned long long> g_launches;
+inline void count_launch(unsigned long long n = 1) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+
+int sm_count();
+
+constexpr uint32_t kDefaultMaxSteps = 4096;
+constexpr int kDefaultBlock = 256;
+constexpr uint32_t kFifoSpinLimit = 1u << 20;   // bounded waits in the free list
+
+}  // namespace pbm
+
+struct pbm_pool {
+    pbm::PoolView view;
+    uint64_t n_pages;
+    uint32_t page_size;
+    uint32_t flags;
+    uint32_t max_slots;
+    size_t bitmap_bytes;            // n_words32 (even) * 4
+    uint64_t padding_bits;          // set bits past n_pages
+    uint32_t* d_words;
+    char* d_base;
+    pbm::DevStats* d_stats;
+    int32_t* d_cursors;             // clustered walk, per slot
+    uint32_t* d_arms;               // distributed clock, per slot
+    unsigned long long* d_arm;      // single clock
+    int32_t* d_ring;                // FIFO ring, n_pages entries (lazily built)
+    pbm::FifoState* d_fifo;
+    bool fifo_valid;
+    uint32_t* d_seen;               // check scratch: one bit per page
+    pbm::CheckCounters* d_check;
+    unsigned long long* d_scan;     // scratch for prefix sums (per-block partials)
+    unsigned long long* d_prefix;   // batch prefix (n_groups + 1)
+    uint32_t prefix_cap;
+    int device;
+};
+
+#define PBM_CUDA_TRY(expr)                                                          \
+    do {                                                                            \
+        cudaError_t _e = (expr);                                                    \
+        if (_e != cudaSuccess) {                                                    \
+            std::fprintf(stderr, "[pbm] %s failed: %s (%s:%d)\n", #expr,           \
+                         cudaGetErrorString(_e), __FILE__, __LINE__);               \
+            return PBM_ERR_CUDA;                                                    \
+        }                                                                           \
+    } while (0)
+
+#define PBM_LAUNCH_CHECK()                                                          \
+    do {                                                                            \
+        cudaError_t _e = cudaGetLastError();                                        \
+        if (_e != cudaSuccess) {                                                    \
+            std::fprintf(stderr, "[pbm] launch failed: %s (%s:%d)\n",              \
+                         cudaGetErrorString(_e), __FILE__, __LINE__);               \
+            return PBM_ERR_CUDA;                                                    \
+        }                                                                           \
+        pbm::count_launch();                                                        \
+    } while (0)
+
+namespace pbm {
+// Implemented in pool.cu
+int fifo_build(pbm_pool* pool, cudaStream_t s);
+int popcount_used(pbm_pool* pool, uint64_t* used, cudaStream_t s);
+}  // namespace pbm

@@ -1,0 +1,325 @@
+"""ctypes binding of libpbm.so (the C ABI declared in include/pbm.h).
+
+Mirrors the reference's host-side interface for the page allocator --
+initMemoryManagement / resetMemoryManager / getFreePagePercentage /
+prefillBuffer (source/RandomWalkBasic_BM.cuh:15-21) -- on an explicit pool
+handle, plus the batch, graph and check entry points.  Device buffers are
+passed as raw device pointers (ints) or as objects with ``data_ptr()``
+(e.g. torch tensors); streams as raw cudaStream_t values (0 = default).
+
+There is no CPU fallback: if libpbm.so is missing or fails to load, the
+import raises.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+from ctypes import (POINTER, Structure, byref, c_char_p, c_double, c_int, c_int32,
+                    c_int64, c_size_t, c_uint32, c_uint64, c_void_p)
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "lib", "libpbm.so")
+
+OK = 0
+ERR_INVALID = -1
+ERR_CUDA = -2
+ERR_NOMEM = -3
+ERR_EXHAUSTED = -4
+ERR_TIMEOUT = -5
+ERR_UNSUPPORTED = -6
+ERR_CORRUPT = -7
+
+RANDOM_WALK = 0
+RANDOM_WALK_BM = 1
+COLLAB_RW_BM = 2
+CLUSTERED_RW_BM = 3
+LINKED_LIST = 4
+SINGLE_CLOCK = 5
+DIST_CLOCK = 6
+STRATEGY_NAMES = {
+    RANDOM_WALK: "RandomWalk", RANDOM_WALK_BM: "RandomWalk_BM", COLLAB_RW_BM: "CollabRW_BM",
+    CLUSTERED_RW_BM: "ClusteredRandomWalk_BM", LINKED_LIST: "LinkedList",
+    SINGLE_CLOCK: "SingleClock", DIST_CLOCK: "DistClock",
+}
+
+OP_ALLOC, OP_FREE, OP_SWAP = 0, 1, 2
+LAUNCH_PLAIN, LAUNCH_PERSISTENT = 0, 1
+POOL_MATERIALIZE = 1
+
+
+class PoolConfig(Structure):
+    _fields_ = [("n_pages", c_uint64), ("page_size", c_uint32), ("flags", c_uint32),
+                ("max_slots", c_uint32), ("reserved", c_uint32)]
+
+
+class WalkConfig(Structure):
+    _fields_ = [("strategy", c_int32), ("word_bits", c_int32), ("collab_width", c_int32),
+                ("stride", c_uint32), ("max_steps", c_uint32), ("block_size", c_int32),
+                ("blocks_per_sm", c_int32), ("free_merge", c_int32)]
+
+
+class Group(Structure):
+    _fields_ = [("op", c_int32), ("count", c_uint32), ("offset", c_uint64)]
+
+
+class Stats(Structure):
+    _fields_ = [("successes", c_uint64), ("failures", c_uint64), ("steps", c_uint64),
+                ("frees", c_uint64)]
+
+
+class CheckResult(Structure):
+    _fields_ = [("n_ok", c_int64), ("n_failed", c_int64), ("n_out_of_range", c_int64),
+                ("n_duplicates", c_int64), ("n_not_marked", c_int64), ("used_pages", c_int64)]
+
+
+# (name, restype, argtypes) -- every entry point of include/pbm.h
+SIGNATURES = [
+    ("pbm_pool_create", c_int, [POINTER(PoolConfig), POINTER(c_void_p)]),
+    ("pbm_pool_destroy", c_int, [c_void_p]),
+    ("pbm_pool_info", c_int, [c_void_p, POINTER(c_uint64), POINTER(c_uint32), POINTER(c_void_p),
+                              POINTER(c_size_t), POINTER(c_void_p)]),
+    ("pbm_pool_reset", c_int, [c_void_p, c_void_p]),
+    ("pbm_pool_prefill_bernoulli", c_int, [c_void_p, c_double, c_uint64, c_void_p]),
+    ("pbm_pool_used", c_int, [c_void_p, POINTER(c_uint64), c_void_p]),
+    ("pbm_pool_read_bitmap", c_int, [c_void_p, c_void_p, c_size_t, c_void_p]),
+    ("pbm_pool_write_bitmap", c_int, [c_void_p, c_void_p, c_size_t, c_void_p]),
+    ("pbm_pool_stats", c_int, [c_void_p, POINTER(Stats), c_void_p]),
+    ("pbm_alloc", c_int, [c_void_p, POINTER(WalkConfig), c_uint32, c_uint32, c_void_p, c_void_p, c_void_p]),
+    ("pbm_alloc_serial", c_int, [c_void_p, POINTER(WalkConfig), c_uint32, c_uint32, c_void_p, c_void_p,
+                                 c_void_p]),
+    ("pbm_free", c_int, [c_void_p, POINTER(WalkConfig), c_uint32, c_void_p, c_void_p]),
+    ("pbm_alloc_runs", c_int, [c_void_p, c_uint32, c_void_p, c_uint32, c_uint32, c_void_p, c_void_p,
+                               c_void_p]),
+    ("pbm_alloc_runs_serial", c_int, [c_void_p, c_uint32, c_void_p, c_uint32, c_uint32, c_void_p,
+                                      c_void_p, c_void_p]),
+    ("pbm_free_runs", c_int, [c_void_p, c_uint32, c_void_p, c_void_p, c_void_p]),
+    ("pbm_claim_write_free", c_int, [c_void_p, c_uint32, c_uint32, c_uint32, c_int, c_uint32, c_void_p,
+                                     c_void_p, c_void_p]),
+    ("pbm_gather_pages", c_int, [c_void_p, c_void_p, c_uint32, c_uint32, c_void_p, c_void_p]),
+    ("pbm_batch_launch", c_int, [c_void_p, POINTER(WalkConfig), c_void_p, POINTER(Group), c_uint32,
+                                 c_void_p, c_uint64, c_uint32, c_void_p, c_int, c_void_p]),
+    ("pbm_batch_graph_create", c_int, [c_void_p, POINTER(WalkConfig), c_void_p, c_uint32, c_uint32,
+                                       c_void_p, c_uint64, c_uint32, c_void_p, POINTER(c_void_p)]),
+    ("pbm_graph_replay", c_int, [c_void_p, c_void_p]),
+    ("pbm_graph_set_step", c_int, [c_void_p, c_uint32, c_void_p]),
+    ("pbm_graph_destroy", c_int, [c_void_p]),
+    ("pbm_check_ids", c_int, [c_void_p, c_void_p, c_uint32, POINTER(CheckResult), c_void_p]),
+    ("pbm_atomic_ceiling", c_int, [c_uint32, c_uint32, c_uint32, c_int, POINTER(c_double),
+                                   POINTER(c_double)]),
+    ("pbm_version", c_char_p, []),
+    ("pbm_kernel_launches", c_uint64, []),
+    ("pbm_device_sm_count", c_int, [POINTER(c_int)]),
+]
+
+
+def load(path: str = LIB_PATH) -> ctypes.CDLL:
+    if not os.path.exists(path):
+        raise RuntimeError(f"libpbm.so not built at {path}; run __graft_entry__.build()")
+    lib = ctypes.CDLL(path)
+    for name, res, args in SIGNATURES:
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    return lib
+
+
+_LIB = None
+
+
+def lib() -> ctypes.CDLL:
+    global _LIB
+    if _LIB is None:
+        _LIB = load()
+    return _LIB
+
+
+class PbmError(RuntimeError):
+    def __init__(self, fn, rc):
+        super().__init__(f"{fn} returned {rc}")
+        self.rc = rc
+
+
+def _ptr(x):
+    if x is None:
+        return None
+    if isinstance(x, int):
+        return x
+    return x.data_ptr()
+
+
+def _check(fn, rc, allow=()):
+    if rc != OK and rc not in allow:
+        raise PbmError(fn, rc)
+    return rc
+
+
+def walk_config(strategy=COLLAB_RW_BM, word_bits=32, collab_width=32, stride=1, max_steps=4096,
+                block_size=256, blocks_per_sm=0, free_merge=1) -> WalkConfig:
+    return WalkConfig(strategy, word_bits, collab_width, stride, max_steps, block_size, blocks_per_sm,
+                      free_merge)
+
+
+class Pool:
+    """An explicit page pool (the reference's implicit per-TU pool as a handle)."""
+
+    def __init__(self, n_pages: int, page_size: int = 4096, materialize: bool = False,
+                 max_slots: int = 0):
+        self.lib = lib()
+        cfg = PoolConfig(n_pages, page_size, POOL_MATERIALIZE if materialize else 0, max_slots, 0)
+        h = c_void_p()
+        _check("pbm_pool_create", self.lib.pbm_pool_create(byref(cfg), byref(h)))
+        self.h = h
+        self.n_pages = n_pages
+        self.page_size = page_size
+        npg, psz, bm, nbytes, base = c_uint64(), c_uint32(), c_void_p(), c_size_t(), c_void_p()
+        _check("pbm_pool_info", self.lib.pbm_pool_info(h, byref(npg), byref(psz), byref(bm),
+                                                       byref(nbytes), byref(base)))
+        self.bitmap_ptr = bm.value
+        self.bitmap_bytes = nbytes.value
+        self.base_ptr = base.value
+
+    def close(self):
+        if self.h:
+            _check("pbm_pool_destroy", self.lib.pbm_pool_destroy(self.h))
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # reference-named host helpers ------------------------------------------------
+    def reset(self, stream=0):
+        """resetMemoryManager()"""
+        _check("pbm_pool_reset", self.lib.pbm_pool_reset(self.h, stream))
+
+    def prefill(self, occupancy: float, seed: int, stream=0):
+        """prefillBuffer(1 - occupancy), as i.i.d. Bernoulli bits"""
+        _check("pbm_pool_prefill_bernoulli",
+               self.lib.pbm_pool_prefill_bernoulli(self.h, occupancy, seed, stream))
+
+    def used(self, stream=0) -> int:
+        out = c_uint64()
+        _check("pbm_pool_used", self.lib.pbm_pool_used(self.h, byref(out), stream))
+        return out.value
+
+    def free_fraction(self, stream=0) -> float:
+        """getFreePagePercentage()"""
+        return (self.n_pages - self.used(stream)) / self.n_pages
+
+    def read_bitmap(self, stream=0):
+        import numpy as np
+        out = np.empty(self.bitmap_bytes // 4, dtype=np.uint32)
+        _check("pbm_pool_read_bitmap",
+               self.lib.pbm_pool_read_bitmap(self.h, out.ctypes.data, self.bitmap_bytes, stream))
+        return out
+
+    def write_bitmap(self, words, stream=0):
+        import numpy as np
+        w = np.ascontiguousarray(words, dtype=np.uint32)
+        assert w.nbytes == self.bitmap_bytes
+        _check("pbm_pool_write_bitmap",
+               self.lib.pbm_pool_write_bitmap(self.h, w.ctypes.data, self.bitmap_bytes, stream))
+
+    def stats(self, stream=0) -> Stats:
+        s = Stats()
+        _check("pbm_pool_stats", self.lib.pbm_pool_stats(self.h, byref(s), stream))
+        return s
+
+    # allocation -----------------------------------------------------------------
+    def alloc(self, cfg: WalkConfig, n: int, seed: int, ids, steps=None, stream=0, serial=False):
+        fn = self.lib.pbm_alloc_serial if serial else self.lib.pbm_alloc
+        return _check("pbm_alloc", fn(self.h, byref(cfg), n, seed, _ptr(ids), _ptr(steps), stream))
+
+    def free(self, cfg: WalkConfig, n: int, ids, stream=0):
+        return _check("pbm_free", self.lib.pbm_free(self.h, byref(cfg), n, _ptr(ids), stream))
+
+    def alloc_runs(self, n, npages, seed, ids, steps=None, max_steps=4096, stream=0, serial=False):
+        fn = self.lib.pbm_alloc_runs_serial if serial else self.lib.pbm_alloc_runs
+        return _check("pbm_alloc_runs", fn(self.h, n, _ptr(npages), seed, max_steps, _ptr(ids),
+                                           _ptr(steps), stream))
+
+    def free_runs(self, n, ids, npages, stream=0):
+        return _check("pbm_free_runs", self.lib.pbm_free_runs(self.h, n, _ptr(ids), _ptr(npages), stream))
+
+    def claim_write_free(self, n, seed, ids, steps=None, payload_bytes=64, hold=False, max_steps=4096,
+                         stream=0):
+        return _check("pbm_claim_write_free",
+                      self.lib.pbm_claim_write_free(self.h, n, seed, payload_bytes, int(hold), max_steps,
+                                                    _ptr(ids), _ptr(steps), stream))
+
+    def gather_pages(self, ids, n, bytes_per_page, out, stream=0):
+        return _check("pbm_gather_pages", self.lib.pbm_gather_pages(self.h, _ptr(ids), n, bytes_per_page,
+                                                                    _ptr(out), stream))
+
+    def batch(self, cfg: WalkConfig, d_groups, h_groups, n_groups, arena, arena_len, seed, mode,
+              steps=None, stream=0):
+        return _check("pbm_batch_launch",
+                      self.lib.pbm_batch_launch(self.h, byref(cfg), _ptr(d_groups), h_groups, n_groups,
+                                                _ptr(arena), arena_len, seed, _ptr(steps), mode, stream))
+
+    def graph(self, cfg: WalkConfig, d_groups, n_groups, n_steps, arena, arena_len, seed0, stream=0):
+        g = c_void_p()
+        _check("pbm_batch_graph_create",
+               self.lib.pbm_batch_graph_create(self.h, byref(cfg), _ptr(d_groups), n_groups, n_steps,
+                                               _ptr(arena), arena_len, seed0, stream, byref(g)))
+        return Graph(self.lib, g)
+
+    def check(self, ids, n, stream=0) -> CheckResult:
+        r = CheckResult()
+        rc = self.lib.pbm_check_ids(self.h, _ptr(ids), n, byref(r), stream)
+        _check("pbm_check_ids", rc, allow=(ERR_CORRUPT,))
+        return r
+
+
+class Graph:
+    def __init__(self, lib_, h):
+        self.lib = lib_
+        self.h = h
+
+    def replay(self, stream=0):
+        _check("pbm_graph_replay", self.lib.pbm_graph_replay(self.h, stream))
+
+    def set_step(self, step, stream=0):
+        _check("pbm_graph_set_step", self.lib.pbm_graph_set_step(self.h, step, stream))
+
+    def close(self):
+        if self.h:
+            self.lib.pbm_graph_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def groups_array(groups):
+    """list of (op, count, offset) -> ctypes Group array"""
+    arr = (Group * len(groups))()
+    for i, (op, count, offset) in enumerate(groups):
+        arr[i] = Group(op, count, offset)
+    return arr
+
+
+def atomic_ceiling(words=1 << 22, threads=152 * 2048, iters=64, returning=1):
+    ops, ms = c_double(), c_double()
+    _check("pbm_atomic_ceiling", lib().pbm_atomic_ceiling(words, threads, iters, returning,
+                                                         byref(ops), byref(ms)))
+    return ops.value, ms.value
+
+
+def kernel_launches() -> int:
+    return lib().pbm_kernel_launches()
+
+
+def version() -> str:
+    return lib().pbm_version().decode()

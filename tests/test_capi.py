@@ -1,0 +1,35 @@
+"""The C-ABI library loads and exports every entry point include/pbm.h
+declares (no device calls: runs without a GPU)."""
+import ctypes
+import os
+import re
+
+from conftest import PKG, ROOT
+
+
+def header_functions():
+    with open(os.path.join(ROOT, "include", "pbm.h")) as f:
+        src = f.read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return sorted(set(re.findall(r"\b(pbm_[a-z0-9_]+)\s*\(", src)))
+
+
+def test_library_exports_every_declared_symbol():
+    import pbm
+
+    lib = ctypes.CDLL(pbm.LIB_PATH)
+    missing = [n for n in header_functions() if not hasattr(lib, n)]
+    assert not missing, missing
+
+
+def test_binding_covers_every_declared_symbol():
+    import pbm
+
+    bound = {n for n, _, _ in pbm.SIGNATURES}
+    assert set(header_functions()) <= bound, set(header_functions()) - bound
+
+
+def test_version_string_without_gpu():
+    import pbm
+
+    assert "sm_103a" in pbm.version()

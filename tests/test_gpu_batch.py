@@ -1,0 +1,128 @@
+"""Batched requests from many caller groups: plain (one launch per group),
+persistent (one launch) and CUDA-graph replay run the same requests and must
+all keep the allocation invariants; single-group persistent launches are
+deterministic replays where the oracle can follow them."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+DT = np.dtype([("op", "<i4"), ("count", "<u4"), ("offset", "<u8")])
+
+
+def _held_arena(orc, T, occ, seed):
+    words = orc.bernoulli_bitmap(T, occ, seed)
+    bits = np.unpackbits(words.view(np.uint8), bitorder="little")[:T]
+    held = np.nonzero(bits)[0].astype(np.int32)
+    np.random.default_rng(seed).shuffle(held)
+    return words, held
+
+
+def _descs(counts, op, start=0, arena_len=1 << 62):
+    tab = np.zeros(len(counts), dtype=DT)
+    cur = start
+    for i, c in enumerate(counts):
+        tab[i] = (op if isinstance(op, int) else op[i], c, cur % arena_len)
+        cur += c
+    return tab
+
+
+@pytest.mark.parametrize("mode", ["plain", "persistent", "graph"])
+@pytest.mark.parametrize("strategy,W,wb", [(2, 32, 32), (2, 16, 64), (1, 32, 32), (0, 32, 32)])
+def test_swap_keeps_occupancy(cuda, pbm_mod, orc, mode, strategy, W, wb):
+    torch = cuda
+    pbm = pbm_mod
+    T, occ, seed = 1 << 20, 0.9, 2
+    pool = pbm.Pool(T, 64)
+    pool.prefill(occ, seed)
+    words, held = _held_arena(orc, T, occ, seed)
+    H = len(held)
+    arena = torch.from_numpy(held).cuda()
+    rng = np.random.default_rng(1)
+    steps = 4
+    counts = np.clip(np.exp(rng.uniform(0, np.log(4097), size=(steps, 64))).astype(np.int64), 1, 4096)
+    tab = np.concatenate([_descs(counts[s], pbm.OP_SWAP, int(counts[:s].sum()), H) for s in range(steps)])
+    d_tab = torch.from_numpy(tab.view(np.uint8).copy()).cuda()
+    cfg = pbm.walk_config(strategy, word_bits=wb, collab_width=W)
+    if mode == "graph":
+        g = pool.graph(cfg, d_tab, 64, steps, arena, H, 500)
+        for _ in range(steps):
+            g.replay()
+        g.close()
+    else:
+        for s in range(steps):
+            rows = tab[s * 64:(s + 1) * 64]
+            hg = pbm.groups_array([(int(r["op"]), int(r["count"]), int(r["offset"])) for r in rows])
+            dg = d_tab[s * 64 * 16:(s + 1) * 64 * 16]
+            pool.batch(cfg, dg, hg, 64, arena, H, 500 + s,
+                       pbm.LAUNCH_PLAIN if mode == "plain" else pbm.LAUNCH_PERSISTENT)
+    torch.cuda.synchronize()
+    st = pool.stats()
+    assert st.failures == 0
+    assert st.successes == int(counts.sum()) == st.frees
+    chk = pool.check(arena, H)
+    assert chk.n_duplicates == 0 and chk.n_out_of_range == 0 and chk.n_not_marked == 0
+    assert chk.n_failed == 0
+    assert chk.used_pages == H          # occupancy unchanged: every held page is in the arena
+    a = arena.cpu().numpy()
+    assert np.unique(a).size == H
+    changed = int((a != held).sum())
+    assert changed == min(H, int(counts.sum()))
+    pool.close()
+
+
+def test_alloc_then_free_groups(cuda, pbm_mod, orc):
+    """ALLOC groups fill an arena, FREE groups release it; mixed ops in one
+    persistent batch keep the invariants and free restores the prefill."""
+    torch = cuda
+    pbm = pbm_mod
+    T = 1 << 18
+    pool = pbm.Pool(T, 64)
+    pool.prefill(0.5, 6)
+    words = orc.bernoulli_bitmap(T, 0.5, 6)
+    base = orc.used_pages(words, T)
+    counts = [1, 33, 1000, 7, 4096, 64, 1, 2048]
+    N = sum(counts)
+    arena = torch.full((N,), -1, dtype=torch.int32, device="cuda")
+    tab = _descs(counts, pbm.OP_ALLOC)
+    d_tab = torch.from_numpy(tab.view(np.uint8).copy()).cuda()
+    cfg = pbm.walk_config(pbm.COLLAB_RW_BM)
+    pool.batch(cfg, d_tab, None, len(counts), arena, N, 9, pbm.LAUNCH_PERSISTENT)
+    chk = pool.check(arena, N)
+    assert chk.n_ok == N and chk.n_duplicates == 0 and chk.used_pages == base + N
+    # free half the groups with FREE, swap the rest (mixed ops in one batch)
+    ops = [pbm.OP_FREE if i % 2 == 0 else pbm.OP_SWAP for i in range(len(counts))]
+    tab2 = _descs(counts, ops)
+    d_tab2 = torch.from_numpy(tab2.view(np.uint8).copy()).cuda()
+    pool.batch(cfg, d_tab2, None, len(counts), arena, N, 10, pbm.LAUNCH_PERSISTENT)
+    n_freed = sum(c for c, o in zip(counts, ops) if o == pbm.OP_FREE)
+    assert pool.used() == base + N - n_freed
+    # free everything that is still held through FREE groups over the swapped slots
+    keep = torch.cat([arena[int(tab2[i]["offset"]):int(tab2[i]["offset"]) + counts[i]]
+                      for i in range(len(counts)) if ops[i] == pbm.OP_SWAP])
+    pool.free(cfg, keep.numel(), keep)
+    assert np.array_equal(pool.read_bitmap(), words)
+    pool.close()
+
+
+def test_single_group_persistent_matches_oracle(cuda, pbm_mod, orc):
+    """One ALLOC group of 32*k requests through the persistent kernel with a
+    pool so sparse that no two warps can race for a word: the result equals
+    the oracle's group-by-group collaborative replay up to warp order, so ids
+    match as a set per warp chunk and the bitmap matches exactly."""
+    torch = cuda
+    pbm = pbm_mod
+    T = 1 << 22
+    pool = pbm.Pool(T, 64)
+    words = orc.empty_bitmap(T)
+    n = 32 * 8
+    arena = torch.full((n,), -1, dtype=torch.int32, device="cuda")
+    tab = _descs([n], pbm.OP_ALLOC)
+    pool.batch(pbm.walk_config(pbm.COLLAB_RW_BM), torch.from_numpy(tab.view(np.uint8).copy()).cuda(),
+               None, 1, arena, n, 33, pbm.LAUNCH_PERSISTENT)
+    exp, _ = orc.replay_alloc(words, T, pbm.COLLAB_RW_BM, n, 33)
+    got = arena.cpu().numpy()
+    for c in range(0, n, 32):
+        assert set(got[c:c + 32]) == set(exp[c:c + 32])
+    assert np.array_equal(pool.read_bitmap(), words)
+    pool.close()

@@ -1,0 +1,110 @@
+"""CPU oracle self-checks (no GPU)."""
+import ctypes
+
+import numpy as np
+import pytest
+
+
+def py_lcg(x):
+    v = 1103515245 * x + 12345
+    r = abs(v) % (1 << 31)
+    r = r if v >= 0 else -r
+    return ((r + (1 << 31)) % (1 << 32)) - (1 << 31)
+
+
+def test_lcg_matches_c_semantics(orc):
+    rng = np.random.default_rng(0)
+    xs = [0, 1, -1, 2**31 - 1, -2**31, 12345, -12345] + list(rng.integers(-2**31, 2**31, 500))
+    for x in xs:
+        assert orc.lcg(int(x)) == py_lcg(int(x))
+
+
+def test_nonnegative_seeds_stay_nonnegative(orc):
+    for r in range(1000):
+        x = orc.seed(5, r)
+        assert 0 <= x < 2**31
+        for _ in range(5):
+            x = orc.lcg(x)
+            assert 0 <= x < 2**31
+
+
+def test_bernoulli_prefill_fraction_and_padding(orc):
+    T = 100_003
+    for occ in (0.0, 0.5, 0.9, 1.0):
+        w = orc.bernoulli_bitmap(T, occ, 7)
+        used = orc.used_pages(w, T)
+        assert abs(used / T - occ) < 0.01
+        bits = np.unpackbits(w.view(np.uint8), bitorder="little")
+        assert bits[T:].all()          # padding held
+
+
+@pytest.mark.parametrize("strategy", [0, 1, 2, 3, 5, 6])
+def test_replay_invariants(orc, strategy):
+    T = 1 << 14
+    w = orc.bernoulli_bitmap(T, 0.6, 3)
+    before = w.copy()
+    kw = {}
+    if strategy == 3:
+        kw["cursors"] = np.full(16, -1, dtype=np.int64)
+    if strategy == 5:
+        kw["arm"] = [0]
+    if strategy == 6:
+        kw["arms"] = np.array([orc.lib().orc_dist_clock_arm0(0, i, T) for i in range(16)], dtype=np.int64)
+    ids, steps = orc.replay_alloc(w, T, strategy, 3000, 4, **kw)
+    c = orc.check_alloc(w, before, T, ids)
+    assert c.n_ok == 3000 and c.n_duplicates == 0 and c.n_not_marked == 0 and c.n_prefilled == 0
+    assert c.used_after == orc.used_pages(before, T) + 3000
+    assert (steps >= 1).all() if strategy != 3 else (steps >= 0).all()
+
+
+@pytest.mark.parametrize("wb,W", [(32, 32), (64, 32), (32, 8), (32, 16), (64, 16)])
+def test_collab_replay_claims_exactly_what_is_needed(orc, wb, W):
+    T = 1 << 14
+    w = orc.bernoulli_bitmap(T, 0.8, 9)
+    before = w.copy()
+    ids, steps = orc.replay_alloc(w, T, 2, 1000, 6, word_bits=wb, collab_width=W)
+    c = orc.check_alloc(w, before, T, ids)
+    assert c.n_ok == 1000 and c.n_duplicates == 0 and c.n_prefilled == 0
+    assert c.used_after == orc.used_pages(before, T) + 1000   # nothing over-claimed
+
+
+def test_checker_catches_planted_duplicate(orc):
+    """A planted mistake (on the CPU, in the oracle's input): a duplicated id
+    and an unmarked id are reported."""
+    T = 4096
+    w = orc.bernoulli_bitmap(T, 0.5, 1)
+    before = w.copy()
+    ids, _ = orc.replay_alloc(w, T, 1, 100, 2)
+    bad = ids.copy()
+    bad[5] = bad[4]
+    free_page = int(np.nonzero(np.unpackbits(w.view(np.uint8), bitorder="little")[:T] == 0)[0][0])
+    bad[7] = free_page
+    c = orc.check_alloc(w, before, T, bad)
+    assert c.n_duplicates == 1 and c.n_not_marked == 1
+
+
+def test_runs_and_fifo(orc):
+    T = 1 << 12
+    w = orc.bernoulli_bitmap(T, 0.2, 2)
+    before = w.copy()
+    k = np.random.default_rng(1).integers(1, 9, size=100)
+    ids, _ = orc.replay_runs(w, T, k, 3)
+    assert (ids >= 0).all() and (((ids & 31) + k) <= 32).all()
+    assert orc.used_pages(w, T) == orc.used_pages(before, T) + int(k.sum())
+    for i, kk in zip(ids, k):
+        orc.lib().orc_free_run(orc.P(w), int(i), int(kk))
+    assert np.array_equal(w, before)
+    assert orc.fifo_replay([3, 5, 9], [("get", None), ("put", 3), ("get", None), ("get", None),
+                                       ("get", None), ("get", None)]) == [3, 5, 9, 3, -1]
+
+
+def test_cpu_churn_keeps_occupancy(orc):
+    T = 1 << 16
+    w = orc.bernoulli_bitmap(T, 0.9, 2)
+    bits = np.unpackbits(w.view(np.uint8), bitorder="little")[:T]
+    held = np.nonzero(bits)[0].astype(np.int32)
+    used0 = orc.used_pages(w, T)
+    secs, ok, fail, st, thr = orc.cpu_churn(w, T, held, 50000, 3, threads=4)
+    assert ok == 50000 and fail == 0
+    assert orc.used_pages(w, T) == used0
+    assert np.unique(held).size == held.size

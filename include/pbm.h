@@ -120,6 +120,27 @@ int pbm_pool_used(pbm_pool *pool, uint64_t *h_used, void *stream);
 /* Snapshot / restore of the bitmap (bytes = bitmap_bytes); synchronous. */
 int pbm_pool_read_bitmap(pbm_pool *pool, void *h_dst, size_t bytes, void *stream);
 int pbm_pool_write_bitmap(pbm_pool *pool, const void *h_src, size_t bytes, void *stream);
+/* Device addresses of a pool's state, for a caller's own kernels (the
+ * drop-in device API in pbm/ *.cuh reads them).  build_fifo != 0 builds the
+ * linked-list strategy's free list from the bitmap first.
+ * [the reference's __device__ globals set by cudaMemcpyToSymbol,
+ * Paging.cuh:69-81, RandomWalkBasic_BM.cuh:47-54, parallelPage.cu:111-146] */
+typedef struct {
+    void    *words;        /* bitmap, bitmap_bytes */
+    void    *base;         /* page memory or NULL */
+    uint64_t n_pages;
+    uint32_t page_size;
+    uint32_t n_words32;
+    uint32_t n_words64;
+    uint32_t max_slots;    /* entries of cursors / arms */
+    void    *cursors;      /* int32[max_slots]: clustered walk, last page per slot (-1 = none) */
+    void    *arms;         /* uint32[max_slots]: distributed clock arms */
+    void    *single_arm;   /* unsigned long long: single clock arm */
+    void    *fifo_state;   /* free-list tickets (see pbm/pbm_device.cuh FifoState) */
+    void    *fifo_ring;    /* int32[n_pages] free-list ring, NULL until built */
+    void    *stats;        /* device statistics block */
+} pbm_device_state;
+int pbm_pool_device_state(pbm_pool *pool, int build_fifo, pbm_device_state *h_out, void *stream);
 /* Accumulated device statistics since create/reset (synchronises `stream`). */
 int pbm_pool_stats(pbm_pool *pool, pbm_stats *h_out, void *stream);
 

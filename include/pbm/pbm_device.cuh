@@ -31,6 +31,26 @@ struct PoolView {
     uint32_t  page_size;  // bytes
 };
 
+// Device statistics block (one per pool), updated with block-aggregated atomics.
+struct DevStats {
+    unsigned long long successes;
+    unsigned long long failures;
+    unsigned long long steps;
+    unsigned long long frees;
+    unsigned long long timeouts;   // bounded waits that gave up
+    unsigned long long pad[3];
+};
+
+// FIFO free list of the linked-list strategy: a ring of page ids with
+// ticket counters.  `avail` is a signed count stored in two's complement.
+struct FifoState {
+    unsigned long long head;   // next get ticket
+    unsigned long long tail;   // next put ticket
+    unsigned long long avail;  // free pages in the ring
+    unsigned long long pad;
+};
+
+constexpr uint32_t kFifoSpinLimit = 1u << 20;   // bounded waits in the free list
 constexpr uint32_t kFull32 = 0xffffffffu;
 constexpr uint64_t kFull64 = 0xffffffffffffffffull;
 
@@ -271,6 +291,77 @@ __device__ __forceinline__ int32_t walk_collab(const PoolView& v, bool need, int
 }
 
 // ---------------------------------------------------------------------------
+// The collaborative walk over an arbitrary set of converged lanes `active`
+// (the drop-in form: the reference's getPage runs on __activemask(),
+// CollabRW_BM.cuh:119).  Active lane k (k-th set bit of `active`) reads word
+// (base + k) mod L; prefix sums use bit-sliced ballots, so inactive lanes
+// never participate.  `slots` = 32 ints of shared memory for this warp.
+// ---------------------------------------------------------------------------
+template <typename Word>
+__device__ __forceinline__ int32_t walk_collab_masked(const PoolView& v, uint32_t active, bool need,
+                                                      int32_t seed, uint32_t max_steps,
+                                                      volatile int32_t* slots, int32_t* steps_out) {
+    using T = WordTraits<Word>;
+    Word* words = reinterpret_cast<Word*>(v.words);
+    const uint32_t L = T::count(v);
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t lt = (1u << lane) - 1u;
+    const uint32_t k = (uint32_t)__popc(active & lt);
+    const uint32_t off = k % L;
+    const bool dedupe = __popc(active) > (int)L;
+    int32_t id = -1;
+    int32_t x = seed;
+    uint32_t needm = __ballot_sync(active, need);
+    uint32_t s = 0;
+    while (needm && s < max_steps) {
+        ++s;
+        x = lcg(x);
+        uint32_t w = idx_hi(x, L) + off;
+        if (w >= L) w -= L;
+        Word val = load_word(words + w);
+        if (dedupe) {
+            uint32_t peers = __match_any_sync(active, w);
+            if ((peers & lt) != 0u) val = T::full();
+        }
+        Word fr = (Word)~val;
+        int cnt = popc_w(fr);
+        int pre = 0;
+#pragma unroll
+        for (int b = 0; b < 7; ++b) pre += __popc(__ballot_sync(active, (cnt >> b) & 1) & lt) << b;
+        int n = __popc(needm);
+        Word m = low_bits(fr, n - pre);
+        Word got = 0;
+        if (m) {
+            Word old = atomic_or(words + w, m);
+            got = m & (Word)~old;
+        }
+        int g = popc_w(got);
+        int gpre = 0, G = 0;
+#pragma unroll
+        for (int b = 0; b < 7; ++b) {
+            uint32_t bm = __ballot_sync(active, (g >> b) & 1);
+            gpre += __popc(bm & lt) << b;
+            G += __popc(bm) << b;
+        }
+        int pos = gpre;
+        while (got) {
+            int b = ctz_w(got);
+            got &= got - (Word)1;
+            slots[pos++] = (int32_t)(((uint32_t)w << T::kShift) + (uint32_t)b);
+        }
+        __syncwarp(active);
+        if (id < 0 && need) {
+            int rank = __popc(needm & lt);
+            if (rank < G) id = slots[rank];
+        }
+        __syncwarp(active);
+        needm = __ballot_sync(active, need && id < 0);
+    }
+    if (steps_out) *steps_out = (int32_t)s;
+    return id;
+}
+
+// ---------------------------------------------------------------------------
 // Clustered walk (CRW_BM, source/CRW_BM.cuh:75-142): resume at the word of
 // this slot's last page (the next word once the last page was the word's
 // top bit) and claim its lowest clear bit; otherwise random word-probe
@@ -405,6 +496,57 @@ __device__ __forceinline__ int32_t walk_run(const PoolView& v, uint32_t n, int32
     }
     if (steps_out) *steps_out = (int32_t)s;
     return -1;
+}
+
+// ---------------------------------------------------------------------------
+// FIFO free list (linked-list strategy, parallelPage.cu:342-440, restated
+// lock-free).  get: reserve one free page on `avail`, take a head ticket,
+// exchange the ring slot with -1 (bounded wait for the put that holds the
+// ticket); put: take a tail ticket, CAS the id into the empty slot (bounded
+// wait).  A wait that runs out records a timeout and returns -1 / false.
+// The bitmap is kept in step so occupancy and invariants read the same.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ int32_t fifo_get(const PoolView& v, FifoState* st, int32_t* ring,
+                                            DevStats* stats, int32_t* spins) {
+    unsigned long long old = atomicAdd(&st->avail, ~0ull);   // avail -= 1
+    if ((long long)old <= 0) {
+        atomicAdd(&st->avail, 1ull);
+        if (spins) *spins = 0;
+        return -1;
+    }
+    unsigned long long t = atomicAdd(&st->head, 1ull);
+    int32_t* slot = ring + (t % v.n_pages);
+    uint32_t k = 0;
+    int32_t id = atomicExch(slot, -1);
+    while (id < 0 && k < kFifoSpinLimit) {
+        __nanosleep(64);
+        ++k;
+        id = atomicExch(slot, -1);
+    }
+    if (spins) *spins = (int32_t)k + 1;
+    if (id < 0) {
+        atomicAdd(&stats->timeouts, 1ull);
+        return -1;
+    }
+    atomicOr(v.words + ((uint32_t)id >> 5), 1u << ((uint32_t)id & 31u));
+    return id;
+}
+
+__device__ __forceinline__ bool fifo_put(const PoolView& v, FifoState* st, int32_t* ring,
+                                         DevStats* stats, int32_t id) {
+    atomicAnd(v.words + ((uint32_t)id >> 5), ~(1u << ((uint32_t)id & 31u)));
+    unsigned long long t = atomicAdd(&st->tail, 1ull);
+    int32_t* slot = ring + (t % v.n_pages);
+    uint32_t k = 0;
+    while (atomicCAS(slot, -1, id) != -1) {
+        if (++k >= kFifoSpinLimit) {
+            atomicAdd(&stats->timeouts, 1ull);
+            return false;
+        }
+        __nanosleep(64);
+    }
+    atomicAdd(&st->avail, 1ull);
+    return true;
 }
 
 // ---------------------------------------------------------------------------

@@ -140,53 +140,6 @@ __global__ void __launch_bounds__(256) k_alloc_collab(AllocArgs a) {
     }
 }
 
-// ---- FIFO free list (linked-list strategy, parallelPage.cu:342-440) ----
-// get: reserve one free page on the counter, take a head ticket, exchange
-// the ring slot with -1 (bounded wait for a put that holds the ticket);
-// put: take a tail ticket, CAS the id into the empty slot (bounded wait).
-__device__ __forceinline__ int32_t fifo_get(const PoolView& v, FifoState* st, int32_t* ring,
-                                            DevStats* stats, int32_t* spins) {
-    unsigned long long old = atomicAdd(&st->avail, ~0ull);   // avail -= 1
-    if ((long long)old <= 0) {
-        atomicAdd(&st->avail, 1ull);
-        *spins = 0;
-        return -1;
-    }
-    unsigned long long t = atomicAdd(&st->head, 1ull);
-    int32_t* slot = ring + (t % v.n_pages);
-    uint32_t k = 0;
-    int32_t id = atomicExch(slot, -1);
-    while (id < 0 && k < kFifoSpinLimit) {
-        __nanosleep(64);
-        ++k;
-        id = atomicExch(slot, -1);
-    }
-    *spins = (int32_t)k + 1;
-    if (id < 0) {
-        atomicAdd(&stats->timeouts, 1ull);
-        return -1;
-    }
-    atomicOr(v.words + ((uint32_t)id >> 5), 1u << ((uint32_t)id & 31u));
-    return id;
-}
-
-__device__ __forceinline__ bool fifo_put(const PoolView& v, FifoState* st, int32_t* ring,
-                                         DevStats* stats, int32_t id) {
-    atomicAnd(v.words + ((uint32_t)id >> 5), ~(1u << ((uint32_t)id & 31u)));
-    unsigned long long t = atomicAdd(&st->tail, 1ull);
-    int32_t* slot = ring + (t % v.n_pages);
-    uint32_t k = 0;
-    while (atomicCAS(slot, -1, id) != -1) {
-        if (++k >= kFifoSpinLimit) {
-            atomicAdd(&stats->timeouts, 1ull);
-            return false;
-        }
-        __nanosleep(64);
-    }
-    atomicAdd(&st->avail, 1ull);
-    return true;
-}
-
 __global__ void __launch_bounds__(256) k_fifo_alloc(AllocArgs a, FifoState* st, int32_t* ring) {
     Acc acc;
     const uint32_t tid = blockIdx.x * blockDim.x + threadIdx.x;

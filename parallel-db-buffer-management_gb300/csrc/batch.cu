@@ -226,14 +226,28 @@ struct pbm_graph {
 
 namespace {
 
+// Resident blocks per SM of a persistent instantiation (queried once per block
+// size, outside any stream capture).
+template <BWalk K, int W, typename Word>
+int persistent_blocks_per_sm(int block) {
+    static int cached_block = 0, cached = 0;
+    if (cached_block != block) {
+        int n = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_batch_persistent<K, W, Word>, block, 0) !=
+            cudaSuccess) {
+            cudaGetLastError();
+            n = 1;
+        }
+        cached = n > 0 ? n : 1;
+        cached_block = block;
+    }
+    return cached;
+}
+
 template <BWalk K, int W, typename Word>
 int launch_batch_kw(const BatchArgs& a, bool persistent, int block, int blocks_per_sm, cudaStream_t s) {
     if (persistent) {
-        int per_sm = blocks_per_sm;
-        if (per_sm <= 0) {
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch_persistent<K, W, Word>, block, 0);
-            if (per_sm <= 0) per_sm = 1;
-        }
+        int per_sm = blocks_per_sm > 0 ? blocks_per_sm : persistent_blocks_per_sm<K, W, Word>(block);
         k_batch_persistent<K, W, Word><<<sm_count() * per_sm, block, 0, s>>>(a);
     } else {
         unsigned long long warps = (a.count + 31ull) / 32ull;
@@ -266,6 +280,26 @@ int launch_batch(const pbm_walk_config* c, const BatchArgs& a, bool persistent, 
     }
     default:
         return PBM_ERR_UNSUPPORTED;
+    }
+}
+
+int resolve_blocks_per_sm(const pbm_walk_config* c) {
+    const int block = c->block_size ? c->block_size : kDefaultBlock;
+    const bool w64 = c->word_bits == 64;
+    switch (c->strategy) {
+    case PBM_RANDOM_WALK: return persistent_blocks_per_sm<BWalk::Page, 32, uint32_t>(block);
+    case PBM_RANDOM_WALK_BM:
+        return w64 ? persistent_blocks_per_sm<BWalk::Word64, 32, uint64_t>(block)
+                   : persistent_blocks_per_sm<BWalk::Word32, 32, uint32_t>(block);
+    default: {
+        const int W = c->collab_width ? c->collab_width : 32;
+        if (W == 8) return w64 ? persistent_blocks_per_sm<BWalk::Collab, 8, uint64_t>(block)
+                               : persistent_blocks_per_sm<BWalk::Collab, 8, uint32_t>(block);
+        if (W == 16) return w64 ? persistent_blocks_per_sm<BWalk::Collab, 16, uint64_t>(block)
+                                : persistent_blocks_per_sm<BWalk::Collab, 16, uint32_t>(block);
+        return w64 ? persistent_blocks_per_sm<BWalk::Collab, 32, uint64_t>(block)
+                   : persistent_blocks_per_sm<BWalk::Collab, 32, uint32_t>(block);
+    }
     }
 }
 
@@ -374,15 +408,31 @@ int pbm_batch_graph_create(pbm_pool* pool, const pbm_walk_config* cfg, const pbm
     a.n_groups = n_groups;
     a.prefix = g->d_prefix;
     a.d_step = g->d_step;
+    // Capture on a private stream (the legacy default stream cannot be
+    // captured); the graph is replayed later on the caller's stream.  The
+    // occupancy query runs before capture.
+    pbm_walk_config c2 = *cfg;
+    if (c2.blocks_per_sm <= 0) c2.blocks_per_sm = resolve_blocks_per_sm(cfg);
+    cudaStream_t cap = nullptr;
+    PBM_CUDA_TRY(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
     const unsigned long long before = g_launches.load();
-    PBM_CUDA_TRY(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
-    k_batch_prefix<<<1, 1024, 0, s>>>(d_groups, n_groups, g->d_step, g->d_prefix);
+    cudaError_t e = cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        cudaStreamDestroy(cap);
+        cudaFree(g->d_step);
+        cudaFree(g->d_prefix);
+        delete g;
+        return PBM_ERR_CUDA;
+    }
+    k_batch_prefix<<<1, 1024, 0, cap>>>(d_groups, n_groups, g->d_step, g->d_prefix);
     count_launch();
-    rc = launch_batch(cfg, a, true, s);
-    k_step_advance<<<1, 32, 0, s>>>(g->d_step);
+    rc = launch_batch(&c2, a, true, cap);
+    k_step_advance<<<1, 32, 0, cap>>>(g->d_step);
     count_launch();
     cudaGraph_t graph = nullptr;
-    cudaError_t e = cudaStreamEndCapture(s, &graph);
+    e = cudaStreamEndCapture(cap, &graph);
+    cudaStreamDestroy(cap);
     if (rc || e != cudaSuccess) {
         if (graph) cudaGraphDestroy(graph);
         cudaFree(g->d_step);

@@ -10,24 +10,6 @@
 
 namespace pbm {
 
-// Device statistics block (one per pool).
-struct DevStats {
-    unsigned long long successes;
-    unsigned long long failures;
-    unsigned long long steps;
-    unsigned long long frees;
-    unsigned long long timeouts;   // bounded waits that gave up
-    unsigned long long pad[3];
-};
-
-// FIFO free list state (linked-list strategy).
-struct FifoState {
-    unsigned long long head;   // next get ticket
-    unsigned long long tail;   // next put ticket
-    unsigned long long avail;  // free pages, as a signed count in two's complement
-    unsigned long long pad;
-};
-
 // Invariant-check counters.
 struct CheckCounters {
     unsigned long long ok, failed, out_of_range, duplicates, not_marked, used;
@@ -40,7 +22,6 @@ int sm_count();
 
 constexpr uint32_t kDefaultMaxSteps = 4096;
 constexpr int kDefaultBlock = 256;
-constexpr uint32_t kFifoSpinLimit = 1u << 20;   // bounded waits in the free list
 
 }  // namespace pbm
 
@@ -75,6 +56,7 @@ struct pbm_pool {
         if (_e != cudaSuccess) {                                                    \
             std::fprintf(stderr, "[pbm] %s failed: %s (%s:%d)\n", #expr,           \
                          cudaGetErrorString(_e), __FILE__, __LINE__);               \
+            cudaGetLastError(); /* do not leave the error for the next caller */   \
             return PBM_ERR_CUDA;                                                    \
         }                                                                           \
     } while (0)

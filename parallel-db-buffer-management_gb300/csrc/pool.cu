@@ -380,6 +380,29 @@ int pbm_pool_write_bitmap(pbm_pool* pool, const void* h_src, size_t bytes, void*
     return PBM_OK;
 }
 
+int pbm_pool_device_state(pbm_pool* pool, int build_fifo, pbm_device_state* h_out, void* stream) {
+    if (!pool || !h_out) return PBM_ERR_INVALID;
+    if (build_fifo && !pool->fifo_valid) {
+        int rc = fifo_build(pool, (cudaStream_t)stream);
+        if (rc) return rc;
+        PBM_CUDA_TRY(cudaStreamSynchronize((cudaStream_t)stream));
+    }
+    h_out->words = pool->d_words;
+    h_out->base = pool->d_base;
+    h_out->n_pages = pool->n_pages;
+    h_out->page_size = pool->page_size;
+    h_out->n_words32 = pool->view.n_words32;
+    h_out->n_words64 = pool->view.n_words64;
+    h_out->max_slots = pool->max_slots;
+    h_out->cursors = pool->d_cursors;
+    h_out->arms = pool->d_arms;
+    h_out->single_arm = pool->d_arm;
+    h_out->fifo_state = pool->d_fifo;
+    h_out->fifo_ring = pool->d_ring;
+    h_out->stats = pool->d_stats;
+    return PBM_OK;
+}
+
 int pbm_pool_stats(pbm_pool* pool, pbm_stats* h_out, void* stream) {
     if (!pool || !h_out) return PBM_ERR_INVALID;
     cudaStream_t s = (cudaStream_t)stream;

@@ -233,11 +233,13 @@ def test_runs_serial_and_parallel(cuda, pbm_mod, orc):
     T = 1 << 18
     pool = _pool(pbm, T, 0.3, 9)
     before = orc.bernoulli_bitmap(T, 0.3, 9)
-    n = 4000
-    k = rng.integers(1, 17, size=n).astype(np.int32)
+    # runs of 1..8 pages, ending near 33% occupancy, where every size still
+    # finds a fitting word within a few jumps
+    n = 2000
+    k = rng.integers(1, 9, size=n).astype(np.int32)
     dk = torch.from_numpy(k).cuda()
     ids = torch.full((n,), -9, dtype=torch.int32, device="cuda")
-    pool.alloc_runs(n, dk, 18, ids)
+    pool.alloc_runs(n, dk, 18, ids, max_steps=1 << 14)
     h = ids.cpu().numpy()
     assert (h >= 0).all()
     assert (((h & 31) + k) <= 32).all()

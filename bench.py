@@ -74,11 +74,11 @@ def build_descriptors(counts, arena_len, op):
     """pbm_group table: (op int32, count uint32, offset uint64) per group, steps x groups."""
     dt = np.dtype([("op", "<i4"), ("count", "<u4"), ("offset", "<u8")])
     tab = np.zeros(counts.shape, dtype=dt)
-    cursor = 0
-    for s in range(counts.shape[0]):
-        for g in range(counts.shape[1]):
-            tab[s, g] = (op, counts[s, g], cursor)
-            cursor = (cursor + int(counts[s, g])) % arena_len
+    flat = counts.reshape(-1).astype(np.uint64)
+    starts = np.concatenate([[0], np.cumsum(flat)[:-1]]).astype(np.uint64) % np.uint64(arena_len)
+    tab["op"] = op
+    tab["count"] = counts.astype(np.uint32)
+    tab["offset"] = starts.reshape(counts.shape)
     return tab
 
 
@@ -98,7 +98,7 @@ class ClockSampler:
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
-                 "--format=csv,noheader,nounits", "-lms", "100"],
+                 "--format=csv,noheader,nounits", "-lms", "20"],
                 stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
@@ -150,10 +150,11 @@ def run_reference(args, rank):
     np.random.default_rng(PREFILL_SEED).shuffle(held)
     threads = oracle.lib().orc_hw_threads()
     pairs = 1 << 23
-    # warm-up + calibration: size each step to ~2 s of work
+    # calibration: size every step so that warm-up + timed steps take ~90 s
     secs, ok, fail, st, _ = oracle.cpu_churn(words, T_PAGES, held, pairs, SEED0, threads)
     rate = 2 * ok / secs
-    pairs = int(max(1 << 22, min(1 << 30, rate * 2.0 / 2)))
+    per_step_s = 90.0 / max(1, args.steps + args.warmup)
+    pairs = int(max(1 << 18, min(1 << 30, rate * per_step_s / 2)))
     for w in range(args.warmup):
         oracle.cpu_churn(words, T_PAGES, held, pairs, SEED0 + 1 + w, threads)
     tot_ops, tot_s = 0, 0.0
@@ -281,7 +282,7 @@ def run_ours(args, rank, world, local_rank):
 
     # ---- plain: one launch per group ----
     res_plain = timed(lambda s: pool.batch(cfg, None, h_groups(s), N_GROUPS, arena, H, SEED0 + s,
-                                           pbm.LAUNCH_PLAIN, stream=sh), range(args.warmup, n_steps))
+                                           pbm.LAUNCH_PLAIN, stream=sh), range(args.warmup, min(n_steps, args.warmup + 100)))
     p_ms = sum(ms for _, ms in res_plain)
     plain_value = sum(2 * int(pairs_per_step[s]) for s, _ in res_plain) / (p_ms * 1e-3)
 
@@ -290,7 +291,7 @@ def run_ours(args, rank, world, local_rank):
     g_pt = pool.graph(cfg_pt, d_tab, N_GROUPS, n_steps, arena, H, SEED0 + 7777, sh)
     for s in range(args.warmup):
         g_pt.replay(sh)
-    res_pt = timed(lambda s: g_pt.replay(sh), range(args.warmup, n_steps))
+    res_pt = timed(lambda s: g_pt.replay(sh), range(args.warmup, min(n_steps, args.warmup + 100)))
     pt_ms = sum(ms for _, ms in res_pt)
     per_thread_value = sum(2 * int(pairs_per_step[s]) for s, _ in res_pt) / (pt_ms * 1e-3)
 
@@ -317,7 +318,7 @@ def run_ours(args, rank, world, local_rank):
     for s in range(args.warmup):
         e2e_step(s)
     torch.cuda.synchronize()
-    res_e2e = timed(e2e_step, range(args.warmup, n_steps))
+    res_e2e = timed(e2e_step, range(args.warmup, min(n_steps, args.warmup + 100)))
     e_ms = sum(ms for _, ms in res_e2e)
     e2e_value = sum(2 * int(pairs_per_step[s]) for s, _ in res_e2e) / (e_ms * 1e-3) * world
 
@@ -327,7 +328,10 @@ def run_ours(args, rank, world, local_rank):
               and chk.n_failed == 0 and chk.used_pages == H)
 
     # ---- roofline: atomic ceiling and HBM ----
-    ceil_ops, _ = pbm.atomic_ceiling(words=1 << 22, threads=pbm_sms() * 2048, iters=64, returning=1)
+    ceil_line, _ = pbm.atomic_ceiling(words=1 << 22, threads=pbm_sms() * 2048, iters=64, returning=1, pattern=1)
+    ceil_spread, _ = pbm.atomic_ceiling(words=1 << 22, threads=pbm_sms() * 2048, iters=64, returning=1,
+                                        pattern=2)
+    ceil_ops = max(ceil_line, ceil_spread)
     pairs_s = value / 2 / world
     atomic_achieved = 2 * pairs_s          # algorithmic RMWs: one claim + one release per pair
     bytes_per_pair = 16                    # 4 B arena read + 4 B write + 2 x 4 B bitmap RMW
@@ -368,7 +372,7 @@ def run_ours(args, rank, world, local_rank):
         "mean_pairs_per_step": avg_pairs,
         "collab_mean_steps": (st.steps / max(1, st.successes + st.failures)),
         "failures": int(st.failures), "invariants_ok": bool(ok_inv),
-        "atomic_ceiling_ops_s": ceil_ops,
+        "atomic_ceiling_ops_s": {"line": ceil_line, "spread": ceil_spread},
     }
     if rank == 0:
         print(json.dumps(line), flush=True)
@@ -378,6 +382,46 @@ def run_ours(args, rank, world, local_rank):
     if dist:
         dist.barrier()
         dist.destroy_process_group()
+    return 0
+
+
+def run_profile_case(args):
+    """The batched form only, for ncu: the same pool, occupancy and groups as
+    the benchmark, without page memory (the kernel never touches it), L2
+    flushed before every replay."""
+    import torch
+
+    import pbm
+
+    torch.cuda.set_device(0)
+    dev = torch.device("cuda", 0)
+    sh = torch.cuda.current_stream().cuda_stream
+    pool = pbm.Pool(T_PAGES, PAGE_SIZE, materialize=False)
+    pool.prefill(OCCUPANCY, PREFILL_SEED, sh)
+    words = pool.read_bitmap(sh)
+    bits = np.unpackbits(words.view(np.uint8), bitorder="little")[:T_PAGES]
+    held = np.nonzero(bits)[0].astype(np.int32)
+    np.random.default_rng(PREFILL_SEED).shuffle(held)
+    arena = torch.from_numpy(held).to(dev)
+    n_steps = args.warmup + args.steps
+    counts = group_counts(n_steps)
+    tab = build_descriptors(counts, len(held), pbm.OP_SWAP)
+    d_tab = torch.from_numpy(tab.view(np.uint8).reshape(-1).copy()).to(dev)
+    flush = torch.empty(512 << 20, dtype=torch.uint8, device=dev)
+    walk = {"collab32": pbm.walk_config(pbm.COLLAB_RW_BM, word_bits=32, collab_width=32),
+            "collab64": pbm.walk_config(pbm.COLLAB_RW_BM, word_bits=64, collab_width=32),
+            "word32": pbm.walk_config(pbm.RANDOM_WALK_BM, word_bits=32)}[args.profile_walk]
+    graph = pool.graph(walk, d_tab, N_GROUPS, n_steps, arena, len(held), SEED0, sh)
+    for _ in range(n_steps):
+        flush.zero_()
+        graph.replay(sh)
+    torch.cuda.synchronize()
+    chk = pool.check(arena, len(held))
+    print(json.dumps({"profile_case": args.profile_walk, "steps": n_steps,
+                      "pairs": int(counts.sum()), "duplicates": chk.n_duplicates,
+                      "used": chk.used_pages, "held": len(held)}))
+    graph.close()
+    pool.close()
     return 0
 
 
@@ -394,12 +438,16 @@ def pbm_sms():
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=1000)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--profile", action="store_true", help="batched form only (for ncu)")
+    ap.add_argument("--profile-walk", default="collab32", choices=["collab32", "collab64", "word32"])
     args = ap.parse_args()
     rank, world, local_rank = env_rank()
+    if args.profile:
+        return run_profile_case(args)
     if args.impl == "reference":
         return run_reference(args, rank)
     return run_ours(args, rank, world, local_rank)

@@ -204,6 +204,54 @@ int pbm_graph_replay(pbm_graph *g, void *stream);
 int pbm_graph_set_step(pbm_graph *g, uint32_t step, void *stream);
 int pbm_graph_destroy(pbm_graph *g);
 
+/* ---------------- buffer manager with CLOCK replacement ----------------
+ * No reference counterpart: the reference's "_BM" files are bitmap
+ * allocators; its SingleClock / DistClock arms (parallelPage.cu:491-509,
+ * 571-592) sweep a free map.  Here the same sweeps choose eviction victims
+ * for a page table over n_logical pages cached in n_frames frames.  A fetch
+ * pins the frame it returns until pbm_bufmgr_round releases it. */
+#define PBM_BM_SINGLE_CLOCK 0   /* one shared hand */
+#define PBM_BM_DIST_CLOCK   1   /* n_arms private hands, request i uses arm (slot0 + i) % n_arms */
+
+typedef struct pbm_bufmgr pbm_bufmgr;
+typedef struct {
+    uint64_t n_logical;    /* logical pages (page-table entries) */
+    uint32_t n_frames;     /* buffer frames */
+    uint32_t frame_size;   /* bytes per frame (multiple of 16; 0 = metadata only) */
+    int32_t  policy;       /* PBM_BM_SINGLE_CLOCK or PBM_BM_DIST_CLOCK */
+    uint32_t n_arms;       /* hands of the distributed clock (0 = 1) */
+    uint32_t max_sweep;    /* hand steps before a miss gives up (0 = 2*n_frames + 64) */
+    uint32_t reserved;
+} pbm_bufmgr_config;
+
+typedef struct {
+    uint64_t hits, misses, evictions, failures, unpins, bad_unpins, timeouts;
+} pbm_bufmgr_counters;
+
+typedef struct {
+    uint64_t resident;       /* page-table entries that point at a frame */
+    uint64_t mapped_frames;  /* frames holding a page */
+    uint64_t mismatches;     /* entries whose frame does not point back */
+    uint64_t loading;        /* pages left half-loaded */
+    uint64_t pins;           /* total pins held */
+} pbm_bufmgr_check_result;
+
+/* d_backing: n_logical * frame_size bytes copied into a frame on each miss
+ * (NULL = no copy). */
+int pbm_bufmgr_create(const pbm_bufmgr_config *cfg, const void *d_backing, pbm_bufmgr **out);
+int pbm_bufmgr_destroy(pbm_bufmgr *m);
+int pbm_bufmgr_reset(pbm_bufmgr *m, void *stream);
+/* One round: unpin d_frames_of[d_release_idx[j]] for j < n_release, then
+ * fetch d_pages[0..n) into d_frames_out (-1 = no frame).  Request i of the
+ * round uses distributed-clock arm (slot0 + i) % n_arms.  serial != 0: one
+ * thread, releases then fetches in order (deterministic replay). */
+int pbm_bufmgr_round(pbm_bufmgr *m, const int32_t *d_frames_of, const int32_t *d_release_idx,
+                     uint32_t n_release, const int32_t *d_pages, uint32_t n, uint32_t slot0,
+                     int32_t *d_frames_out, int serial, void *stream);
+int pbm_bufmgr_stats(pbm_bufmgr *m, pbm_bufmgr_counters *h_out, void *stream);
+int pbm_bufmgr_check(pbm_bufmgr *m, pbm_bufmgr_check_result *h_out, void *stream);
+int pbm_bufmgr_frames(pbm_bufmgr *m, void **d_frames, size_t *bytes);
+
 /* ---------------- checks and measurement ---------------- */
 
 /* Invariants of an allocation result: ids in range, no page handed to two
@@ -211,10 +259,14 @@ int pbm_graph_destroy(pbm_graph *g);
 int pbm_check_ids(pbm_pool *pool, const int32_t *d_ids, uint32_t n, pbm_check_result *h_out,
                   void *stream);
 
-/* Uncontended atomicOr ceiling: `threads` threads each issue `iters`
- * returning atomicOr operations on distinct words of a `words`-word buffer
- * spread over the L2 slices.  h_ops_per_s <- RMW/s measured with CUDA events. */
-int pbm_atomic_ceiling(uint32_t words, uint32_t threads, uint32_t iters, int returning,
+/* Uncontended atomicOr ceiling (the roofline denominator of the allocation
+ * kernels): `threads` threads each issue `iters` atomicOr operations
+ * (returning = 1: the old value is used) on words no other thread touches in
+ * the same iteration, in a `words`-word buffer.  pattern 1 = the 32 lanes of
+ * a warp hit one 128-byte line, 2 = lanes 33 words apart (32 lines per warp
+ * instruction), 0 = the faster of the two.  h_ops_per_s <- RMW/s from CUDA
+ * events (best of 5).  [precedent: unitTestLinkedList2.cu:3-16] */
+int pbm_atomic_ceiling(uint32_t words, uint32_t threads, uint32_t iters, int returning, int pattern,
                        double *h_ops_per_s, double *h_ms);
 
 /* Library identity and the number of kernels this library has launched. */

@@ -201,6 +201,27 @@ int32_t orc_ref_dist_clock(int32_t *map, int32_t n_pages, int32_t *arms, int32_t
 int32_t orc_ref_dist_clock_arm(int32_t tid, int16_t clk, int32_t n_pages);
 
 /* ------------------------------------------------------------------ */
+/* CLOCK buffer manager, single-thread replay (oracle_bufmgr.c)        */
+/* ------------------------------------------------------------------ */
+typedef struct {
+    int32_t *page_table;     /* frame or -1 */
+    uint64_t *frame_state;   /* (page << 32) | pins */
+    uint8_t *ref;
+    uint32_t *arms;
+    uint64_t hand;
+    uint32_t n_logical, n_frames, max_sweep, n_arms;
+    int dist;
+    uint64_t hits, misses, evictions, failures, unpins, bad_unpins;
+} orc_bm_t;
+void orc_bm_init(orc_bm_t *b, uint32_t n_logical, uint32_t n_frames, uint32_t max_sweep,
+                 uint32_t n_arms, int dist);
+void orc_bm_free(orc_bm_t *b);
+int32_t orc_bm_fetch(orc_bm_t *b, uint32_t page, uint32_t slot);
+void orc_bm_unpin(orc_bm_t *b, int32_t f);
+void orc_bm_round(orc_bm_t *b, const int32_t *frames_of, const int32_t *release_idx, uint32_t n_release,
+                  const int32_t *pages, uint32_t n, uint32_t slot0, int32_t *frames_out);
+
+/* ------------------------------------------------------------------ */
 /* std::atomic host replay (CPU baseline), cpu_replay.cpp              */
 /* ------------------------------------------------------------------ */
 double orc_cpu_churn(uint32_t *words, uint64_t n_pages, int32_t *held, uint64_t n_held,

@@ -1,0 +1,352 @@
+// bufmgr.cu -- buffer manager with CLOCK (second-chance) replacement.
+//
+// The reference has page allocators only; its SingleClock / DistClock arms
+// sweep the free map (parallelPage.cu:491-509, 571-592) but there is no page
+// table, no reference bits and no eviction.  This file defines the buffer
+// manager on those sweep mechanics:
+//
+//   page_table[p]   frame holding logical page p, -1 not resident, -2 being
+//                   loaded by another request
+//   frame_state[f]  (page << 32) | pins in one 64-bit word, so a fetch pins a
+//                   frame only if it still holds its page, and a sweep takes a
+//                   frame only if it is unpinned and unchanged -- each with one
+//                   compare-and-swap
+//   ref[f]          CLOCK reference bit, set on every fetch
+//   arms            SINGLE: one shared hand (atomicAdd); DIST: per-slot hands,
+//                   each starting at its own frame and advancing privately
+//
+// fetch(p): resident -> pin it, set ref (hit).  Not resident -> become its
+// loader (CAS page_table -1 -> -2), sweep: skip pinned frames, clear the
+// reference bit of referenced ones (second chance), take the first unpinned
+// unreferenced frame, unmap its old page (eviction), optionally copy the
+// page from the backing store, map p (miss).  A fetch that finds no frame
+// within max_sweep hand steps fails (-1) instead of spinning; waits on a
+// loading page are bounded too.
+#include <cstring>
+#include <new>
+
+#include "internal.cuh"
+
+namespace pbm {
+namespace {
+
+constexpr uint32_t kEmptyPage = 0xffffffffu;
+constexpr int32_t kLoading = -2;
+constexpr uint32_t kFetchSpinLimit = 1u << 16;
+
+struct BmStats {
+    unsigned long long hits, misses, evictions, failures, unpins, bad_unpins, timeouts, pad;
+};
+
+struct BmView {
+    int32_t* page_table;
+    unsigned long long* frame_state;
+    uint8_t* ref;
+    unsigned long long* single_hand;
+    uint32_t* arms;
+    const char* backing;     // n_logical * frame_size bytes, may be null
+    char* frames;            // n_frames * frame_size bytes, may be null
+    BmStats* stats;
+    uint32_t n_logical;
+    uint32_t n_frames;
+    uint32_t frame_size;
+    uint32_t max_sweep;
+    uint32_t n_arms;
+    int32_t dist;            // 0 = single hand, 1 = per-slot hands
+};
+
+__device__ __forceinline__ uint32_t next_frame(const BmView& b, uint32_t slot, uint32_t* arm_local) {
+    if (!b.dist) return (uint32_t)(atomicAdd(b.single_hand, 1ull) % b.n_frames);
+    uint32_t a = *arm_local;
+    uint32_t f = a >= b.n_frames ? a - b.n_frames : a;
+    *arm_local = f + 1u;
+    return f;
+}
+
+// Victim search; returns a frame now holding (page, 1 pin) and its old page.
+__device__ __forceinline__ int32_t sweep(const BmView& b, uint32_t page, uint32_t slot, uint32_t* old_page) {
+    uint32_t arm = b.dist ? b.arms[slot] : 0u;
+    int32_t out = -1;
+    for (uint32_t i = 0; i < b.max_sweep; ++i) {
+        uint32_t f = next_frame(b, slot, &arm);
+        unsigned long long s = __ldcg(b.frame_state + f);
+        if ((uint32_t)s != 0u) continue;                    // pinned
+        if (b.ref[f]) { b.ref[f] = 0; continue; }           // second chance
+        unsigned long long ns = ((unsigned long long)page << 32) | 1ull;
+        if (atomicCAS(b.frame_state + f, s, ns) == s) {
+            *old_page = (uint32_t)(s >> 32);
+            out = (int32_t)f;
+            break;
+        }
+    }
+    if (b.dist) b.arms[slot] = arm;
+    return out;
+}
+
+struct BmAcc {
+    unsigned long long hits = 0, misses = 0, evictions = 0, failures = 0, timeouts = 0;
+};
+
+__device__ __forceinline__ int32_t fetch(const BmView& b, uint32_t page, uint32_t slot, BmAcc& acc) {
+    for (uint32_t attempt = 0; attempt < kFetchSpinLimit; ++attempt) {
+        int32_t f = __ldcg(b.page_table + page);
+        if (f >= 0) {
+            unsigned long long s = __ldcg(b.frame_state + f);
+            while ((uint32_t)(s >> 32) == page) {
+                unsigned long long old = atomicCAS(b.frame_state + f, s, s + 1ull);
+                if (old == s) {
+                    b.ref[f] = 1;
+                    ++acc.hits;
+                    return f;
+                }
+                s = old;
+            }
+            continue;   // the frame changed owner: read the page table again
+        }
+        if (f == -1) {
+            if (atomicCAS(b.page_table + page, -1, kLoading) != -1) continue;
+            uint32_t old_page = kEmptyPage;
+            int32_t h = sweep(b, page, slot, &old_page);
+            if (h < 0) {
+                atomicExch(b.page_table + page, -1);
+                ++acc.failures;
+                return -1;
+            }
+            if (old_page != kEmptyPage) {
+                atomicExch(b.page_table + old_page, -1);
+                ++acc.evictions;
+            }
+            if (b.backing && b.frames) {
+                const int4* src = reinterpret_cast<const int4*>(b.backing + (size_t)page * b.frame_size);
+                int4* dst = reinterpret_cast<int4*>(b.frames + (size_t)h * b.frame_size);
+                for (uint32_t k = 0; k < b.frame_size / 16u; ++k) dst[k] = src[k];
+            }
+            b.ref[h] = 1;
+            __threadfence();
+            atomicExch(b.page_table + page, h);
+            ++acc.misses;
+            return h;
+        }
+        __nanosleep(32);   // another request is loading this page
+    }
+    ++acc.timeouts;
+    return -1;
+}
+
+__device__ __forceinline__ void unpin(const BmView& b, int32_t f, unsigned long long& ok, unsigned long long& bad) {
+    if (f < 0 || (uint32_t)f >= b.n_frames) return;
+    unsigned long long s = __ldcg(b.frame_state + f);
+    for (;;) {
+        if ((uint32_t)s == 0u) { ++bad; return; }
+        unsigned long long old = atomicCAS(b.frame_state + f, s, s - 1ull);
+        if (old == s) { ++ok; return; }
+        s = old;
+    }
+}
+
+// One round: release the listed pins, then fetch this round's pages.
+// With one thread this is the deterministic replay of the round.
+__global__ void __launch_bounds__(256) k_round(BmView b, const int32_t* release_frames_of,
+                                               const int32_t* release_idx, uint32_t n_release,
+                                               const int32_t* pages, uint32_t n, uint32_t slot0,
+                                               int32_t* frames_out) {
+    const uint32_t tid = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t nthr = gridDim.x * blockDim.x;
+    unsigned long long ok = 0, bad = 0;
+    for (uint32_t j = tid; j < n_release; j += nthr) {
+        int32_t idx = release_idx[j];
+        unpin(b, release_frames_of[idx], ok, bad);
+    }
+    if (nthr == 1u) __threadfence();
+    BmAcc acc;
+    for (uint32_t i = tid; i < n; i += nthr) {
+        int32_t p = pages[i];
+        int32_t f = -1;
+        if (p >= 0 && (uint32_t)p < b.n_logical) f = fetch(b, (uint32_t)p, (slot0 + i) % b.n_arms, acc);
+        frames_out[i] = f;
+    }
+    if (ok) atomicAdd(&b.stats->unpins, ok);
+    if (bad) atomicAdd(&b.stats->bad_unpins, bad);
+    if (acc.hits) atomicAdd(&b.stats->hits, acc.hits);
+    if (acc.misses) atomicAdd(&b.stats->misses, acc.misses);
+    if (acc.evictions) atomicAdd(&b.stats->evictions, acc.evictions);
+    if (acc.failures) atomicAdd(&b.stats->failures, acc.failures);
+    if (acc.timeouts) atomicAdd(&b.stats->timeouts, acc.timeouts);
+}
+
+__global__ void k_bm_init(BmView b) {
+    const uint32_t tid = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t nthr = gridDim.x * blockDim.x;
+    for (uint32_t p = tid; p < b.n_logical; p += nthr) b.page_table[p] = -1;
+    for (uint32_t f = tid; f < b.n_frames; f += nthr) {
+        b.frame_state[f] = (unsigned long long)kEmptyPage << 32;
+        b.ref[f] = 0;
+    }
+    for (uint32_t a = tid; a < b.n_arms; a += nthr)
+        b.arms[a] = (uint32_t)(((unsigned long long)a * b.n_frames) / b.n_arms);
+    if (tid == 0) *b.single_hand = 0ull;
+}
+
+// Consistency check: page_table and frame_state are inverse maps; pins sum.
+struct BmCheck {
+    unsigned long long resident, mapped_frames, mismatches, loading, pins;
+};
+
+__global__ void k_bm_check(BmView b, BmCheck* out) {
+    const uint32_t tid = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t nthr = gridDim.x * blockDim.x;
+    unsigned long long res = 0, mapped = 0, mism = 0, loading = 0, pins = 0;
+    for (uint32_t p = tid; p < b.n_logical; p += nthr) {
+        int32_t f = b.page_table[p];
+        if (f == kLoading) { ++loading; continue; }
+        if (f < 0) continue;
+        ++res;
+        if ((uint32_t)f >= b.n_frames || (uint32_t)(b.frame_state[f] >> 32) != p) ++mism;
+    }
+    for (uint32_t f = tid; f < b.n_frames; f += nthr) {
+        unsigned long long s = b.frame_state[f];
+        uint32_t pg = (uint32_t)(s >> 32);
+        pins += (uint32_t)s;
+        if (pg == kEmptyPage) continue;
+        ++mapped;
+        if (pg >= b.n_logical || b.page_table[pg] != (int32_t)f) ++mism;
+    }
+    if (res) atomicAdd(&out->resident, res);
+    if (mapped) atomicAdd(&out->mapped_frames, mapped);
+    if (mism) atomicAdd(&out->mismatches, mism);
+    if (loading) atomicAdd(&out->loading, loading);
+    if (pins) atomicAdd(&out->pins, pins);
+}
+
+}  // namespace
+}  // namespace pbm
+
+using namespace pbm;
+
+struct pbm_bufmgr {
+    BmView v;
+    BmCheck* d_check;
+    size_t frames_bytes;
+};
+
+extern "C" {
+
+int pbm_bufmgr_create(const pbm_bufmgr_config* cfg, const void* d_backing, pbm_bufmgr** out) {
+    if (!cfg || !out || cfg->n_logical == 0 || cfg->n_logical > 0x7fffffffull || cfg->n_frames == 0 ||
+        cfg->n_frames >= 0x7fffffffu || (cfg->frame_size % 16u) != 0 || cfg->policy < 0 || cfg->policy > 1)
+        return PBM_ERR_INVALID;
+    *out = nullptr;
+    pbm_bufmgr* m = new (std::nothrow) pbm_bufmgr();
+    if (!m) return PBM_ERR_NOMEM;
+    std::memset((void*)m, 0, sizeof(*m));
+    BmView& b = m->v;
+    b.n_logical = (uint32_t)cfg->n_logical;
+    b.n_frames = cfg->n_frames;
+    b.frame_size = cfg->frame_size;
+    b.max_sweep = cfg->max_sweep ? cfg->max_sweep : 2u * cfg->n_frames + 64u;
+    b.n_arms = cfg->n_arms ? cfg->n_arms : 1u;
+    b.dist = cfg->policy;
+    b.backing = (const char*)d_backing;
+    bool ok = cudaMalloc(&b.page_table, sizeof(int32_t) * b.n_logical) == cudaSuccess &&
+              cudaMalloc(&b.frame_state, sizeof(unsigned long long) * b.n_frames) == cudaSuccess &&
+              cudaMalloc(&b.ref, b.n_frames) == cudaSuccess &&
+              cudaMalloc(&b.single_hand, sizeof(unsigned long long)) == cudaSuccess &&
+              cudaMalloc(&b.arms, sizeof(uint32_t) * b.n_arms) == cudaSuccess &&
+              cudaMalloc(&b.stats, sizeof(BmStats)) == cudaSuccess &&
+              cudaMalloc(&m->d_check, sizeof(BmCheck)) == cudaSuccess;
+    if (ok && cfg->frame_size) {
+        m->frames_bytes = (size_t)b.n_frames * cfg->frame_size;
+        ok = cudaMalloc(&b.frames, m->frames_bytes) == cudaSuccess;
+    }
+    if (!ok) {
+        cudaGetLastError();
+        pbm_bufmgr_destroy(m);
+        return PBM_ERR_NOMEM;
+    }
+    int rc = pbm_bufmgr_reset(m, nullptr);
+    if (rc == PBM_OK && cudaDeviceSynchronize() != cudaSuccess) rc = PBM_ERR_CUDA;
+    if (rc) { pbm_bufmgr_destroy(m); return rc; }
+    *out = m;
+    return PBM_OK;
+}
+
+int pbm_bufmgr_destroy(pbm_bufmgr* m) {
+    if (!m) return PBM_ERR_INVALID;
+    cudaDeviceSynchronize();
+    cudaFree(m->v.page_table);
+    cudaFree(m->v.frame_state);
+    cudaFree(m->v.ref);
+    cudaFree(m->v.single_hand);
+    cudaFree(m->v.arms);
+    cudaFree(m->v.stats);
+    cudaFree(m->v.frames);
+    cudaFree(m->d_check);
+    delete m;
+    return PBM_OK;
+}
+
+int pbm_bufmgr_reset(pbm_bufmgr* m, void* stream) {
+    if (!m) return PBM_ERR_INVALID;
+    cudaStream_t s = (cudaStream_t)stream;
+    k_bm_init<<<sm_count() * 4, 256, 0, s>>>(m->v);
+    PBM_LAUNCH_CHECK();
+    PBM_CUDA_TRY(cudaMemsetAsync(m->v.stats, 0, sizeof(BmStats), s));
+    return PBM_OK;
+}
+
+int pbm_bufmgr_round(pbm_bufmgr* m, const int32_t* d_frames_of, const int32_t* d_release_idx,
+                     uint32_t n_release, const int32_t* d_pages, uint32_t n, uint32_t slot0,
+                     int32_t* d_frames_out, int serial, void* stream) {
+    if (!m || (n_release && (!d_frames_of || !d_release_idx)) || (n && (!d_pages || !d_frames_out)))
+        return PBM_ERR_INVALID;
+    if (n == 0 && n_release == 0) return PBM_OK;
+    const uint32_t work = n > n_release ? n : n_release;
+    int block = serial ? 1 : 256;
+    int grid = serial ? 1 : (int)((work + 255u) / 256u);
+    k_round<<<grid, block, 0, (cudaStream_t)stream>>>(m->v, d_frames_of, d_release_idx, n_release, d_pages,
+                                                       n, slot0, d_frames_out);
+    PBM_LAUNCH_CHECK();
+    return PBM_OK;
+}
+
+int pbm_bufmgr_stats(pbm_bufmgr* m, pbm_bufmgr_counters* h_out, void* stream) {
+    if (!m || !h_out) return PBM_ERR_INVALID;
+    cudaStream_t s = (cudaStream_t)stream;
+    BmStats d;
+    PBM_CUDA_TRY(cudaMemcpyAsync(&d, m->v.stats, sizeof(d), cudaMemcpyDeviceToHost, s));
+    PBM_CUDA_TRY(cudaStreamSynchronize(s));
+    h_out->hits = d.hits;
+    h_out->misses = d.misses;
+    h_out->evictions = d.evictions;
+    h_out->failures = d.failures;
+    h_out->unpins = d.unpins;
+    h_out->bad_unpins = d.bad_unpins;
+    h_out->timeouts = d.timeouts;
+    return (d.timeouts || d.bad_unpins) ? PBM_ERR_CORRUPT : PBM_OK;
+}
+
+int pbm_bufmgr_check(pbm_bufmgr* m, pbm_bufmgr_check_result* h_out, void* stream) {
+    if (!m || !h_out) return PBM_ERR_INVALID;
+    cudaStream_t s = (cudaStream_t)stream;
+    PBM_CUDA_TRY(cudaMemsetAsync(m->d_check, 0, sizeof(BmCheck), s));
+    k_bm_check<<<sm_count() * 4, 256, 0, s>>>(m->v, m->d_check);
+    PBM_LAUNCH_CHECK();
+    BmCheck c;
+    PBM_CUDA_TRY(cudaMemcpyAsync(&c, m->d_check, sizeof(c), cudaMemcpyDeviceToHost, s));
+    PBM_CUDA_TRY(cudaStreamSynchronize(s));
+    h_out->resident = c.resident;
+    h_out->mapped_frames = c.mapped_frames;
+    h_out->mismatches = c.mismatches;
+    h_out->loading = c.loading;
+    h_out->pins = c.pins;
+    return (c.mismatches || c.loading || c.resident != c.mapped_frames) ? PBM_ERR_CORRUPT : PBM_OK;
+}
+
+int pbm_bufmgr_frames(pbm_bufmgr* m, void** d_frames, size_t* bytes) {
+    if (!m) return PBM_ERR_INVALID;
+    if (d_frames) *d_frames = m->v.frames;
+    if (bytes) *bytes = m->frames_bytes;
+    return PBM_OK;
+}
+
+}  // extern "C"

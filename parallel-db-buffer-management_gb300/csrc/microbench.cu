@@ -63,8 +63,9 @@ static int time_one(uint32_t* buf, uint32_t mask, uint32_t threads, uint32_t ite
 using namespace pbm;
 
 extern "C" int pbm_atomic_ceiling(uint32_t words, uint32_t threads, uint32_t iters, int returning,
-                                  double* h_ops_per_s, double* h_ms) {
-    if (!h_ops_per_s || words < 1024 || (words & (words - 1)) || threads == 0 || iters == 0)
+                                  int pattern, double* h_ops_per_s, double* h_ms) {
+    if (!h_ops_per_s || words < 1024 || (words & (words - 1)) || threads == 0 || iters == 0 ||
+        pattern < 0 || pattern > 2)
         return PBM_ERR_INVALID;
     uint32_t* buf = nullptr;
     uint32_t* sink = nullptr;
@@ -74,10 +75,12 @@ extern "C" int pbm_atomic_ceiling(uint32_t words, uint32_t threads, uint32_t ite
         return PBM_ERR_NOMEM;
     }
     PBM_CUDA_TRY(cudaMemset(buf, 0, (size_t)words * 4u));
-    float t_line = 0, t_spread = 0;
-    int rc = returning ? time_one<true, false>(buf, words - 1u, threads, iters, sink, &t_line)
+    float t_line = 1e30f, t_spread = 1e30f;
+    int rc = PBM_OK;
+    if (pattern != 2)
+        rc = returning ? time_one<true, false>(buf, words - 1u, threads, iters, sink, &t_line)
                        : time_one<false, false>(buf, words - 1u, threads, iters, sink, &t_line);
-    if (!rc)
+    if (!rc && pattern != 1)
         rc = returning ? time_one<true, true>(buf, words - 1u, threads, iters, sink, &t_spread)
                        : time_one<false, true>(buf, words - 1u, threads, iters, sink, &t_spread);
     cudaFree(buf);

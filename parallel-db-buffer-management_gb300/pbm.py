@@ -72,6 +72,31 @@ class CheckResult(Structure):
                 ("n_duplicates", c_int64), ("n_not_marked", c_int64), ("used_pages", c_int64)]
 
 
+class DeviceState(Structure):
+    _fields_ = [("words", c_void_p), ("base", c_void_p), ("n_pages", c_uint64), ("page_size", c_uint32),
+                ("n_words32", c_uint32), ("n_words64", c_uint32), ("max_slots", c_uint32),
+                ("cursors", c_void_p), ("arms", c_void_p), ("single_arm", c_void_p),
+                ("fifo_state", c_void_p), ("fifo_ring", c_void_p), ("stats", c_void_p)]
+
+
+BM_SINGLE_CLOCK, BM_DIST_CLOCK = 0, 1
+
+
+class BufMgrConfig(Structure):
+    _fields_ = [("n_logical", c_uint64), ("n_frames", c_uint32), ("frame_size", c_uint32),
+                ("policy", c_int32), ("n_arms", c_uint32), ("max_sweep", c_uint32), ("reserved", c_uint32)]
+
+
+class BufMgrCounters(Structure):
+    _fields_ = [("hits", c_uint64), ("misses", c_uint64), ("evictions", c_uint64), ("failures", c_uint64),
+                ("unpins", c_uint64), ("bad_unpins", c_uint64), ("timeouts", c_uint64)]
+
+
+class BufMgrCheck(Structure):
+    _fields_ = [("resident", c_uint64), ("mapped_frames", c_uint64), ("mismatches", c_uint64),
+                ("loading", c_uint64), ("pins", c_uint64)]
+
+
 # (name, restype, argtypes) -- every entry point of include/pbm.h
 SIGNATURES = [
     ("pbm_pool_create", c_int, [POINTER(PoolConfig), POINTER(c_void_p)]),
@@ -84,6 +109,7 @@ SIGNATURES = [
     ("pbm_pool_read_bitmap", c_int, [c_void_p, c_void_p, c_size_t, c_void_p]),
     ("pbm_pool_write_bitmap", c_int, [c_void_p, c_void_p, c_size_t, c_void_p]),
     ("pbm_pool_stats", c_int, [c_void_p, POINTER(Stats), c_void_p]),
+    ("pbm_pool_device_state", c_int, [c_void_p, c_int, POINTER(DeviceState), c_void_p]),
     ("pbm_alloc", c_int, [c_void_p, POINTER(WalkConfig), c_uint32, c_uint32, c_void_p, c_void_p, c_void_p]),
     ("pbm_alloc_serial", c_int, [c_void_p, POINTER(WalkConfig), c_uint32, c_uint32, c_void_p, c_void_p,
                                  c_void_p]),
@@ -104,8 +130,16 @@ SIGNATURES = [
     ("pbm_graph_set_step", c_int, [c_void_p, c_uint32, c_void_p]),
     ("pbm_graph_destroy", c_int, [c_void_p]),
     ("pbm_check_ids", c_int, [c_void_p, c_void_p, c_uint32, POINTER(CheckResult), c_void_p]),
-    ("pbm_atomic_ceiling", c_int, [c_uint32, c_uint32, c_uint32, c_int, POINTER(c_double),
+    ("pbm_atomic_ceiling", c_int, [c_uint32, c_uint32, c_uint32, c_int, c_int, POINTER(c_double),
                                    POINTER(c_double)]),
+    ("pbm_bufmgr_create", c_int, [POINTER(BufMgrConfig), c_void_p, POINTER(c_void_p)]),
+    ("pbm_bufmgr_destroy", c_int, [c_void_p]),
+    ("pbm_bufmgr_reset", c_int, [c_void_p, c_void_p]),
+    ("pbm_bufmgr_round", c_int, [c_void_p, c_void_p, c_void_p, c_uint32, c_void_p, c_uint32, c_uint32,
+                                 c_void_p, c_int, c_void_p]),
+    ("pbm_bufmgr_stats", c_int, [c_void_p, POINTER(BufMgrCounters), c_void_p]),
+    ("pbm_bufmgr_check", c_int, [c_void_p, POINTER(BufMgrCheck), c_void_p]),
+    ("pbm_bufmgr_frames", c_int, [c_void_p, POINTER(c_void_p), POINTER(c_size_t)]),
     ("pbm_version", c_char_p, []),
     ("pbm_kernel_launches", c_uint64, []),
     ("pbm_device_sm_count", c_int, [POINTER(c_int)]),
@@ -302,6 +336,52 @@ class Graph:
             pass
 
 
+class BufferManager:
+    """Page table over n_logical pages cached in n_frames frames, CLOCK replacement."""
+
+    def __init__(self, n_logical, n_frames, frame_size=0, policy=BM_SINGLE_CLOCK, n_arms=1, max_sweep=0,
+                 backing=None):
+        self.lib = lib()
+        cfg = BufMgrConfig(n_logical, n_frames, frame_size, policy, n_arms, max_sweep, 0)
+        h = c_void_p()
+        _check("pbm_bufmgr_create", self.lib.pbm_bufmgr_create(byref(cfg), _ptr(backing), byref(h)))
+        self.h = h
+
+    def round(self, frames_of, release_idx, n_release, pages, n, slot0, frames_out, serial=False, stream=0):
+        return _check("pbm_bufmgr_round",
+                      self.lib.pbm_bufmgr_round(self.h, _ptr(frames_of), _ptr(release_idx), n_release,
+                                                _ptr(pages), n, slot0, _ptr(frames_out), int(serial), stream))
+
+    def reset(self, stream=0):
+        _check("pbm_bufmgr_reset", self.lib.pbm_bufmgr_reset(self.h, stream))
+
+    def counters(self, stream=0) -> BufMgrCounters:
+        c = BufMgrCounters()
+        _check("pbm_bufmgr_stats", self.lib.pbm_bufmgr_stats(self.h, byref(c), stream), allow=(ERR_CORRUPT,))
+        return c
+
+    def check(self, stream=0) -> BufMgrCheck:
+        c = BufMgrCheck()
+        _check("pbm_bufmgr_check", self.lib.pbm_bufmgr_check(self.h, byref(c), stream), allow=(ERR_CORRUPT,))
+        return c
+
+    def frames(self):
+        p, n = c_void_p(), c_size_t()
+        _check("pbm_bufmgr_frames", self.lib.pbm_bufmgr_frames(self.h, byref(p), byref(n)))
+        return p.value, n.value
+
+    def close(self):
+        if self.h:
+            self.lib.pbm_bufmgr_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 def groups_array(groups):
     """list of (op, count, offset) -> ctypes Group array"""
     arr = (Group * len(groups))()
@@ -310,9 +390,10 @@ def groups_array(groups):
     return arr
 
 
-def atomic_ceiling(words=1 << 22, threads=152 * 2048, iters=64, returning=1):
+def atomic_ceiling(words=1 << 22, threads=152 * 2048, iters=64, returning=1, pattern=0):
+    """RMW/s of uncontended atomicOr; pattern 1 = one line per warp, 2 = 32 lines, 0 = best."""
     ops, ms = c_double(), c_double()
-    _check("pbm_atomic_ceiling", lib().pbm_atomic_ceiling(words, threads, iters, returning,
+    _check("pbm_atomic_ceiling", lib().pbm_atomic_ceiling(words, threads, iters, returning, pattern,
                                                          byref(ops), byref(ms)))
     return ops.value, ms.value
 

@@ -130,6 +130,8 @@ SIGNATURES = [
     ("pbm_graph_set_step", c_int, [c_void_p, c_uint32, c_void_p]),
     ("pbm_graph_destroy", c_int, [c_void_p]),
     ("pbm_check_ids", c_int, [c_void_p, c_void_p, c_uint32, POINTER(CheckResult), c_void_p]),
+    ("pbm_check_ids_noalloc", c_int, [c_void_p, c_uint64, c_void_p, c_uint32, POINTER(CheckResult),
+                                      c_void_p]),
     ("pbm_atomic_ceiling", c_int, [c_uint32, c_uint32, c_uint32, c_int, c_int, POINTER(c_double),
                                    POINTER(c_double)]),
     ("pbm_bufmgr_create", c_int, [POINTER(BufMgrConfig), c_void_p, POINTER(c_void_p)]),

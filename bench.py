@@ -182,7 +182,7 @@ def workload_config():
         "workload": "alloc+free churn at 90% occupancy: 2^24 x 4 KiB pages (64 GiB), 256 caller groups/step "
                     "with LogU[1,65536] requests (seed 4), swap op on a resident held-page arena",
         "pool_pages": T_PAGES, "page_size": PAGE_SIZE, "occupancy": OCCUPANCY, "prefill_seed": PREFILL_SEED,
-        "groups_per_step": N_GROUPS, "walk": "CollabRW_BM, 32 lanes, 32-bit words, merged frees",
+        "groups_per_step": N_GROUPS, "walk": "autotuned for the 90% band (see tuned_config); reference arm: word-probe walk",
         "launch": "persistent kernel in a CUDA graph", "l2": "flushed between timed steps (512 MiB write)",
         "parallelism": "single GPU per rank (independent pools)",
     }
@@ -231,7 +231,17 @@ def run_ours(args, rank, world, local_rank):
     tab = build_descriptors(counts, H, pbm.OP_SWAP)
     d_tab = torch.from_numpy(tab.view(np.uint8).reshape(-1).copy()).to(dev)
     flush = torch.empty(512 << 20, dtype=torch.uint8, device=dev)
+    # autotuner (untimed): candidates run on step 0's groups, swaps keep the pool at 90%
+    tuned = pool.autotune(d_tab[:N_GROUPS * 16], N_GROUPS, int(counts[0].sum()), arena, H, seed=SEED0 - 999,
+                          reps=4, stream=sh)
+    torch.cuda.synchronize()
     cfg = pbm.walk_config(pbm.COLLAB_RW_BM, word_bits=32, collab_width=32, free_merge=1)
+    if tuned:
+        cfg = pbm.WalkConfig.from_buffer_copy(tuned[0].cfg)
+
+    def cfg_dict(c):
+        return {"walk": pbm.STRATEGY_NAMES[c.strategy], "word_bits": c.word_bits, "width": c.collab_width,
+                "stride": c.stride, "blocks_per_sm": c.blocks_per_sm, "free_merge": c.free_merge}
 
     def h_groups(s):
         return pbm.groups_array([(pbm.OP_SWAP, int(tab[s, g]["count"]), int(tab[s, g]["offset"]))
@@ -361,7 +371,7 @@ def run_ours(args, rank, world, local_rank):
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": g_ms / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic",
-        "config": workload_config(),
+        "config": dict(workload_config(), walk=cfg_dict(cfg)),
         "plain_value": plain_value, "batched_over_plain": value / world / plain_value,
         "per_thread_walk_value": per_thread_value,
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(np.mean(e2e_bytes_in)),
@@ -373,6 +383,8 @@ def run_ours(args, rank, world, local_rank):
         "collab_mean_steps": (st.steps / max(1, st.successes + st.failures)),
         "failures": int(st.failures), "invariants_ok": bool(ok_inv),
         "atomic_ceiling_ops_s": {"line": ceil_line, "spread": ceil_spread},
+        "tuned_config": cfg_dict(cfg),
+        "autotune_top": [dict(cfg_dict(t.cfg), ops_per_s=t.ops_per_s) for t in tuned[:6]],
     }
     if rank == 0:
         print(json.dumps(line), flush=True)

@@ -47,10 +47,13 @@ extern "C" {
 #define PBM_OP_FREE    1   /* free ids[i] (ids < 0 are skipped) */
 #define PBM_OP_SWAP    2   /* allocate a new page, free ids[i], ids[i] <- new page
                               (on failure ids[i] keeps its page) */
+#define PBM_OP_MALLOC  3   /* malloc batches: ptrs[i] <- block of sizes[i] bytes (0 on failure) */
+#define PBM_OP_MFREE   4   /* malloc batches: free ptrs[i] (0 = nothing), ptrs[i] <- 0 */
 
 /* ---- launch forms ---- */
 #define PBM_LAUNCH_PLAIN       0   /* one kernel launch per group */
 #define PBM_LAUNCH_PERSISTENT  1   /* one persistent kernel over all groups */
+#define PBM_LAUNCH_SERIAL      2   /* malloc batches: one warp, requests in order (deterministic replay) */
 
 /* Pool flags */
 #define PBM_POOL_MATERIALIZE   1u  /* also reserve n_pages*page_size bytes of page memory */
@@ -204,6 +207,50 @@ int pbm_graph_replay(pbm_graph *g, void *stream);
 int pbm_graph_set_step(pbm_graph *g, uint32_t step, void *stream);
 int pbm_graph_destroy(pbm_graph *g);
 
+/* ---------------- size-classed malloc over the pool's pages ----------------
+ * [mallocRW / freeRW, RWMalloc.cuh:299-334; MemoryManager::malloc / free,
+ * malloc.cuh:3-37, malloc.cu:223-320].  Sizes round up to power-of-two
+ * classes 16 B .. 64 KiB; the sub-page requests of each group of 32
+ * consecutive requests share one run of pages (largest class first, so each
+ * sub-page block is aligned to its size); larger requests take their own
+ * run and start on a page boundary; the
+ * last free of a run releases it.  Needs a materialised pool with a
+ * power-of-two page size in 2 KiB .. 64 KiB. */
+int pbm_malloc_init(pbm_pool *pool);     /* side tables: 9 bytes per page */
+int pbm_malloc_release(pbm_pool *pool);
+/* Device addresses of the malloc side tables (int32 start_of[T], int32
+ * live[T], uint8 len_of[T]) for a caller's own kernels (pbm/pbm_malloc.cuh). */
+int pbm_malloc_tables(pbm_pool *pool, void **d_start_of, void **d_live, void **d_len_of);
+/* Groups use PBM_OP_MALLOC / PBM_OP_MFREE; slot i of a group is arena slot
+ * (offset + i) mod arena_len of d_sizes (uint32 bytes) and d_ptrs (device
+ * addresses).  mode: PBM_LAUNCH_PLAIN (h_groups needed), _PERSISTENT or _SERIAL. */
+int pbm_malloc_batch(pbm_pool *pool, const pbm_group *d_groups, const pbm_group *h_groups, uint32_t n_groups,
+                     const uint32_t *d_sizes, unsigned long long *d_ptrs, uint64_t arena_len, uint32_t seed,
+                     uint32_t max_steps, int mode, void *stream);
+/* Graph form: step k reads d_groups + k*n_groups with seed seed0 + k. */
+int pbm_malloc_graph_create(pbm_pool *pool, const pbm_group *d_groups, uint32_t n_groups, uint32_t n_steps,
+                            const uint32_t *d_sizes, unsigned long long *d_ptrs, uint64_t arena_len,
+                            uint32_t seed0, uint32_t max_steps, void *stream, pbm_graph **out);
+/* Runs still holding blocks, and frees rejected so far (outside the pool or
+ * double frees); synchronous. */
+int pbm_malloc_counts(pbm_pool *pool, uint64_t *h_live_runs, uint64_t *h_bad_frees, void *stream);
+
+/* Autotuner (no reference counterpart).  Runs the caller's batch of
+ * `requests` swap requests (descriptors in d_groups, all PBM_OP_SWAP) through
+ * the persistent kernel for every candidate configuration -- walk, width
+ * 8/16/32, 32/64-bit words, stride, blocks per SM, merged frees -- `reps`
+ * times each, and returns up to max_out results sorted fastest first.  Swaps
+ * keep the pool's occupancy, so tune once per occupancy band. */
+typedef struct {
+    pbm_walk_config cfg;
+    float ms_per_batch;
+    float reserved;
+    double ops_per_s;      /* 2 * requests / time (one alloc + one free each) */
+} pbm_tune_result;
+int pbm_autotune(pbm_pool *pool, const pbm_group *d_groups, uint32_t n_groups, uint64_t requests,
+                 int32_t *d_arena, uint64_t arena_len, uint32_t seed, int reps, uint32_t max_steps,
+                 pbm_tune_result *h_out, uint32_t max_out, uint32_t *h_n_out, void *stream);
+
 /* ---------------- buffer manager with CLOCK replacement ----------------
  * No reference counterpart: the reference's "_BM" files are bitmap
  * allocators; its SingleClock / DistClock arms (parallelPage.cu:491-509,
@@ -251,6 +298,69 @@ int pbm_bufmgr_round(pbm_bufmgr *m, const int32_t *d_frames_of, const int32_t *d
 int pbm_bufmgr_stats(pbm_bufmgr *m, pbm_bufmgr_counters *h_out, void *stream);
 int pbm_bufmgr_check(pbm_bufmgr *m, pbm_bufmgr_check_result *h_out, void *stream);
 int pbm_bufmgr_frames(pbm_bufmgr *m, void **d_frames, size_t *bytes);
+/* Copies the first bytes_per_frame bytes of each listed frame into d_out
+ * (ids < 0 give zeros). */
+int pbm_bufmgr_gather(pbm_bufmgr *m, const int32_t *d_frame_ids, uint32_t n, uint32_t bytes_per_frame,
+                      int32_t *d_out, void *stream);
+
+/* ---------------- serving loop (no reference counterpart) ----------------
+ * Continuous batching of many tenants' requests over one resident pool (and
+ * buffer manager for fetches).  pbm_server_run replays the requests in real
+ * time from their arrival stamps (seconds from the start of the run, sorted).
+ * ALLOC n: n new pages appended to the tenant's ring of page slots.
+ * FREE n:  releases min(n, pages the tenant holds) of its oldest pages.
+ * FETCH n: pins then releases the next n pages of the shared fetch trace.
+ * A tenant's requests are admitted in arrival order; an ALLOC waits until
+ * held pages stay <= max_occupancy of the pool, a FREE until the pages it
+ * releases are allocated on the device.  Admitted requests of all tenants
+ * form the next batch whenever one of n_streams batch slots is free, so
+ * batches overlap on the device.  Page counts per request depend only on
+ * the tenant's own requests (results do not depend on the mix). */
+#define PBM_REQ_ALLOC 0
+#define PBM_REQ_FREE  1
+#define PBM_REQ_FETCH 2
+
+typedef struct {
+    double   arrival_s;
+    uint32_t tenant;
+    int32_t  op;           /* PBM_REQ_* */
+    uint32_t count;        /* pages */
+    uint32_t reserved;
+} pbm_request;
+
+typedef struct {
+    double   admit_s, launch_s, done_s, latency_s;   /* seconds since the run started */
+    uint64_t pages;        /* pages allocated / released / fetched */
+    int32_t  status;       /* 0 done, -1 never admitted */
+    uint32_t reserved;
+} pbm_request_result;
+
+typedef struct {
+    uint32_t n_tenants;
+    uint32_t ring_pages;          /* page slots per tenant */
+    uint32_t n_streams;           /* batches in flight at most */
+    uint32_t max_batch_requests;  /* requests per batch at most (<= 2048) */
+    uint32_t max_fetch_pages;     /* fetch pages per batch at most (0 = 1<<22) */
+    uint32_t reserved;
+    double   max_occupancy;       /* admission bound on held pages / pool pages */
+    double   drain_timeout_s;     /* stop waiting this long after the last arrival */
+    pbm_walk_config walk;         /* allocation walk of the batches */
+} pbm_server_config;
+
+typedef struct {
+    uint64_t requests, completed, rejected, pages, batches, max_in_flight;
+    double   wall_s, p50_s, p99_s, mean_batch_requests;
+} pbm_server_report;
+
+typedef struct pbm_server pbm_server;
+/* bm may be NULL when no request fetches; d_fetch_pages: logical page ids. */
+int pbm_server_create(pbm_pool *pool, pbm_bufmgr *bm, const int32_t *d_fetch_pages, uint64_t n_fetch_pages,
+                      const pbm_server_config *cfg, pbm_server **out);
+int pbm_server_run(pbm_server *s, const pbm_request *h_reqs, uint64_t n, pbm_request_result *h_results,
+                   pbm_server_report *h_report);
+/* Pages a tenant holds now, oldest first (h_out may be NULL to get the count). */
+int pbm_server_tenant_pages(pbm_server *s, uint32_t tenant, int32_t *h_out, uint64_t max_out, uint64_t *h_n);
+int pbm_server_destroy(pbm_server *s);
 
 /* ---------------- checks and measurement ---------------- */
 

@@ -31,6 +31,9 @@ __host__ inline void initMemoryManagement(int nGB = TOTAL_SIZE_GB_DEFAULT, int p
                              false, &pbm_tu_host, &ds);
     h_total_n_pages = (int)pbm_tu_host.n_pages;
     cudaMemcpyToSymbol(pbm_tu_state, &ds, sizeof(ds));
+#ifdef PBM_DROPIN_AFTER_INIT
+    PBM_DROPIN_AFTER_INIT();   // family-specific set-up (RWMalloc.cuh: malloc tables)
+#endif
 }
 
 /* pageAddress / getPageID: Paging.cuh:30-52 (one contiguous reservation) */

@@ -38,7 +38,8 @@ struct DevStats {
     unsigned long long steps;
     unsigned long long frees;
     unsigned long long timeouts;   // bounded waits that gave up
-    unsigned long long pad[3];
+    unsigned long long bad_frees;  // malloc frees rejected (outside the pool / double free)
+    unsigned long long pad[2];
 };
 
 // FIFO free list of the linked-list strategy: a ring of page ids with
@@ -65,6 +66,14 @@ __host__ __device__ __forceinline__ int32_t lcg(int32_t x) {
     long long v = 1103515245LL * (long long)x + 12345LL;
     long long r = v >= 0 ? (v & 0x7fffffffLL) : -((-v) & 0x7fffffffLL);
     return (int32_t)r;
+}
+
+// The same step for a state in [0, 2^31), which is every state the walks
+// see (request seeds are 31-bit and the LCG keeps non-negative states
+// non-negative): (A*x + C) mod 2^31 is then the low 31 bits of the 32-bit
+// product, so one multiply-add and a mask replace the 64-bit arithmetic.
+__host__ __device__ __forceinline__ int32_t lcg31(int32_t x) {
+    return (int32_t)((1103515245u * (uint32_t)x + 12345u) & 0x7fffffffu);
 }
 
 // Index in [0, n) from the LCG state's 31 bits by multiply-high.  The
@@ -153,11 +162,11 @@ template <> struct WordTraits<uint64_t> {
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ int32_t walk_page(const PoolView& v, int32_t seed0,
                                              uint32_t max_steps, int32_t* steps_out) {
-    int32_t x = seed0;
+    int32_t x = seed0 & 0x7fffffff;   // walks run on 31-bit states
     uint32_t s = 0;
     while (s < max_steps) {
         ++s;
-        x = lcg(x);
+        x = lcg31(x);
         uint32_t p = idx_hi(x, v.n_pages);
         uint32_t* wp = v.words + (p >> 5);
         uint32_t bit = 1u << (p & 31u);
@@ -183,11 +192,11 @@ __device__ __forceinline__ int32_t walk_word(const PoolView& v, int32_t seed0,
     using T = WordTraits<Word>;
     Word* words = reinterpret_cast<Word*>(v.words);
     const uint32_t L = T::count(v);
-    int32_t x = seed0;
+    int32_t x = seed0 & 0x7fffffff;   // walks run on 31-bit states
     uint32_t s = 0;
     while (s < max_steps) {
         ++s;
-        x = lcg(x);
+        x = lcg31(x);
         uint32_t w = idx_hi(x, L);
         Word val = load_word(words + w);
         while (val != T::full()) {
@@ -234,12 +243,12 @@ __device__ __forceinline__ int32_t walk_collab(const PoolView& v, bool need, int
     const uint32_t gmask = (W == 32) ? kFull32 : (((1u << W) - 1u) << (lane & ~(uint32_t)(W - 1)));
     const uint32_t lt = (1u << lane) - 1u;                           // lanes below me
     int32_t id = -1;
-    int32_t x = group_seed;
+    int32_t x = group_seed & 0x7fffffff;
     uint32_t needm = __ballot_sync(gmask, need);
     uint32_t s = 0;
     while (needm && s < max_steps) {
         ++s;
-        x = lcg(x);
+        x = lcg31(x);
         uint32_t w = idx_hi(x, L) + lane_off;
         if (w >= L) w -= L;
         Word val = load_word(words + w);
@@ -265,13 +274,21 @@ __device__ __forceinline__ int32_t walk_collab(const PoolView& v, bool need, int
             got = m & (Word)~old;
         }
         int g = popc_w(got);
-        int gincl = g;
+        int gincl, G;
+        if (__ballot_sync(gmask, got != m) == 0u) {
+            // every planned bit stuck: lane i gained exactly its share, so the
+            // prefix of gains is the capped prefix of free bits
+            gincl = min(incl, n);
+            G = min(__shfl_sync(gmask, incl, W - 1, W), n);
+        } else {
+            gincl = g;
 #pragma unroll
-        for (int d = 1; d < W; d <<= 1) {
-            int y = __shfl_up_sync(gmask, gincl, d, W);
-            if ((int)gl >= d) gincl += y;
+            for (int d = 1; d < W; d <<= 1) {
+                int y = __shfl_up_sync(gmask, gincl, d, W);
+                if ((int)gl >= d) gincl += y;
+            }
+            G = __shfl_sync(gmask, gincl, W - 1, W);
         }
-        int G = __shfl_sync(gmask, gincl, W - 1, W);
         int pos = gincl - g;
         while (got) {
             int b = ctz_w(got);
@@ -310,12 +327,12 @@ __device__ __forceinline__ int32_t walk_collab_masked(const PoolView& v, uint32_
     const uint32_t off = k % L;
     const bool dedupe = __popc(active) > (int)L;
     int32_t id = -1;
-    int32_t x = seed;
+    int32_t x = seed & 0x7fffffff;
     uint32_t needm = __ballot_sync(active, need);
     uint32_t s = 0;
     while (needm && s < max_steps) {
         ++s;
-        x = lcg(x);
+        x = lcg31(x);
         uint32_t w = idx_hi(x, L) + off;
         if (w >= L) w -= L;
         Word val = load_word(words + w);
@@ -390,9 +407,9 @@ __device__ __forceinline__ int32_t walk_crw(const PoolView& v, int32_t* cursor, 
             val = old | bit;
         }
     }
-    int32_t x = seed0;
+    int32_t x = seed0 & 0x7fffffff;   // walks run on 31-bit states
     for (uint32_t j = 0; j < max_steps; ++j) {
-        x = lcg(x);
+        x = lcg31(x);
         uint32_t w = idx_hi(x, L);
         uint32_t val = load_word(v.words + w);
         while (val != kFull32) {
@@ -474,11 +491,11 @@ __device__ __forceinline__ uint32_t run_starts(uint32_t f, uint32_t n) {
 __device__ __forceinline__ int32_t walk_run(const PoolView& v, uint32_t n, int32_t seed0,
                                             uint32_t max_steps, int32_t* steps_out) {
     const uint32_t L = v.n_words32;
-    int32_t x = seed0;
+    int32_t x = seed0 & 0x7fffffff;   // walks run on 31-bit states
     uint32_t s = 0;
     while (s < max_steps) {
         ++s;
-        x = lcg(x);
+        x = lcg31(x);
         uint32_t w = idx_hi(x, L);
         uint32_t val = load_word(v.words + w);
         for (int tries = 0; tries < 64; ++tries) {

@@ -220,3 +220,72 @@ def fifo_replay(free_pages_sorted, ops):
         else:
             q.append(int(arg))
     return out
+
+
+class BmT(Structure):
+    _fields_ = [("page_table", c_void_p), ("frame_state", c_void_p), ("ref", c_void_p), ("arms", c_void_p),
+                ("hand", c_uint64), ("n_logical", c_uint32), ("n_frames", c_uint32), ("max_sweep", c_uint32),
+                ("n_arms", c_uint32), ("dist", c_int), ("hits", c_uint64), ("misses", c_uint64),
+                ("evictions", c_uint64), ("failures", c_uint64), ("unpins", c_uint64), ("bad_unpins", c_uint64)]
+
+
+class BufMgrReplay:
+    """Single-thread replay of the CLOCK buffer manager (oracle_bufmgr.c)."""
+
+    def __init__(self, n_logical, n_frames, max_sweep=0, n_arms=1, dist=0):
+        L = lib()
+        L.orc_bm_init.argtypes = [ctypes.POINTER(BmT), c_uint32, c_uint32, c_uint32, c_uint32, c_int]
+        L.orc_bm_free.argtypes = [ctypes.POINTER(BmT)]
+        L.orc_bm_round.argtypes = [ctypes.POINTER(BmT), _P, _P, c_uint32, _P, c_uint32, c_uint32, _P]
+        self.L = L
+        self.b = BmT()
+        L.orc_bm_init(ctypes.byref(self.b), n_logical, n_frames, max_sweep, n_arms, dist)
+
+    def round(self, frames_of, release_idx, pages, slot0):
+        frames_out = np.empty(len(pages), dtype=np.int32)
+        self.L.orc_bm_round(ctypes.byref(self.b), P(frames_of), P(release_idx), len(release_idx),
+                            P(pages), len(pages), slot0, P(frames_out))
+        return frames_out
+
+    def counters(self):
+        b = self.b
+        return dict(hits=b.hits, misses=b.misses, evictions=b.evictions, failures=b.failures,
+                    unpins=b.unpins, bad_unpins=b.bad_unpins)
+
+    def close(self):
+        if self.b.page_table:
+            self.L.orc_bm_free(ctypes.byref(self.b))
+
+
+class MallocT(Structure):
+    _fields_ = [("words", c_void_p), ("n_pages", c_uint32), ("page_shift", c_uint32), ("start_of", c_void_p),
+                ("live", c_void_p), ("len_of", c_void_p)]
+
+
+class MallocReplay:
+    """Sequential replay of the size-classed malloc (oracle_malloc.c) on a
+    bitmap the caller owns (mutated in place)."""
+
+    def __init__(self, words, n_pages, page_shift):
+        L = lib()
+        L.orc_malloc_group.argtypes = [ctypes.POINTER(MallocT), _P, c_int, c_int32, _P, c_uint32, _P, _P]
+        L.orc_malloc_free.argtypes = [ctypes.POINTER(MallocT), ctypes.c_int64]
+        L.orc_malloc_free.restype = c_int
+        self.L = L
+        self.words = words
+        self.start_of = np.full(n_pages, -1, dtype=np.int32)
+        self.live = np.zeros(n_pages, dtype=np.int32)
+        self.len_of = np.zeros(n_pages, dtype=np.uint8)
+        self.m = MallocT(P(words), n_pages, page_shift, P(self.start_of), P(self.live), P(self.len_of))
+
+    def group(self, sizes, seed_small, seed_own, max_steps=4096):
+        sizes = np.ascontiguousarray(sizes, dtype=np.uint64)
+        seed_own = np.ascontiguousarray(seed_own, dtype=np.int32)
+        offs = np.zeros(len(sizes), dtype=np.int64)
+        steps = np.zeros(len(sizes), dtype=np.int32)
+        self.L.orc_malloc_group(ctypes.byref(self.m), P(sizes), len(sizes), seed_small, P(seed_own), max_steps,
+                                P(offs), P(steps))
+        return offs, steps
+
+    def free(self, offset):
+        return self.L.orc_malloc_free(ctypes.byref(self.m), int(offset))

@@ -222,6 +222,24 @@ void orc_bm_round(orc_bm_t *b, const int32_t *frames_of, const int32_t *release_
                   const int32_t *pages, uint32_t n, uint32_t slot0, int32_t *frames_out);
 
 /* ------------------------------------------------------------------ */
+/* Size-classed malloc, sequential replay (oracle_malloc.c)            */
+/* ------------------------------------------------------------------ */
+typedef struct {
+    uint32_t *words;       /* pool bitmap */
+    uint32_t n_pages;
+    uint32_t page_shift;
+    int32_t *start_of;     /* [n_pages] */
+    int32_t *live;         /* [n_pages] */
+    uint8_t *len_of;       /* [n_pages] */
+} orc_malloc_t;
+/* One group of `lanes` requests; offsets[l] = byte offset of the block from
+ * the pool base, or -1. */
+void orc_malloc_group(orc_malloc_t *m, const uint64_t *sizes, int lanes, int32_t seed_small,
+                      const int32_t *seed_own, uint32_t max_steps, int64_t *offsets, int32_t *steps);
+/* 1 = freed, 0 = rejected (outside the pool or no live block). */
+int orc_malloc_free(orc_malloc_t *m, int64_t offset);
+
+/* ------------------------------------------------------------------ */
 /* std::atomic host replay (CPU baseline), cpu_replay.cpp              */
 /* ------------------------------------------------------------------ */
 double orc_cpu_churn(uint32_t *words, uint64_t n_pages, int32_t *held, uint64_t n_held,

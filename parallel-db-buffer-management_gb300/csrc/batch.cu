@@ -11,7 +11,7 @@
 //   graph       the persistent form captured once in a CUDA graph together
 //               with its prefix kernel and a step-advance kernel, so each
 //               replay reads the next step's descriptors from device memory.
-#include "internal.cuh"
+#include "batch_common.cuh"
 
 namespace pbm {
 
@@ -21,12 +21,14 @@ struct BatchArgs {
     PoolView v;
     const pbm_group* groups;            // base of the descriptor table
     uint32_t n_groups;
-    const uint32_t* d_step;             // graph form: step counter (may be null)
+    uint32_t* d_step;                   // graph form: step counter (may be null)
     uint32_t seed;
     int32_t* arena;
     unsigned long long arena_len;
     int32_t* steps;                     // parallel to arena, may be null
-    const unsigned long long* prefix;   // persistent: n_groups + 1 exclusive prefix
+    const unsigned long long* prefix;   // persistent, not fused: n_groups + 1 exclusive prefix
+    int32_t fuse;                       // persistent: each block scans the groups itself
+    uint32_t* done;                     // graph form: blocks finished (last one advances d_step)
     uint32_t max_steps;
     uint32_t stride;
     int32_t dedupe;
@@ -113,14 +115,36 @@ __device__ __forceinline__ void batch_round(const BatchArgs& a, uint32_t seed, b
     else if (to_free >= 0) free_page(a.v, to_free);
 }
 
-template <BWalk K, int W, typename Word>
-__global__ void __launch_bounds__(256) k_batch_persistent(BatchArgs a) {
+__device__ __forceinline__ unsigned long long wrap_slot(unsigned long long slot, unsigned long long len) {
+    if (slot >= len) slot = slot - len < len ? slot - len : slot % len;
+    return slot;
+}
+
+__device__ __forceinline__ void prefetch_l2(const void* p) {
+    asm volatile("prefetch.global.L2 [%0];" ::"l"(p));
+}
+
+// The persistent batch kernel.  With a.fuse each block scans the step's
+// group counts into shared memory itself (no separate prefix kernel); with
+// a.done the last block to finish advances the graph's step counter (no
+// separate step kernel), so one graph replay is one launch.  While a chunk is
+// processed, lane 0 prefetches into L2 the next chunk's arena slots and the
+// first bitmap line its walk will read.
+template <BWalk K, int W, typename Word, int MINB>
+__global__ void __launch_bounds__(256, MINB) k_batch_persistent(BatchArgs a) {
+    extern __shared__ unsigned long long s_prefix[];
     __shared__ int32_t slots[256];
+    __shared__ bool s_last;
     BAcc acc;
     const uint32_t step = a.d_step ? *a.d_step : 0u;
     const pbm_group* groups = a.groups + (size_t)step * a.n_groups;
     const uint32_t seed = a.seed + step;
-    const unsigned long long total = a.prefix[a.n_groups];
+    const unsigned long long* pre = a.prefix;
+    if (a.fuse) {
+        block_exclusive_prefix(groups, a.n_groups, s_prefix);
+        pre = s_prefix;
+    }
+    const unsigned long long total = pre[a.n_groups];
     const uint32_t lane = threadIdx.x & 31u;
     const uint32_t gl = threadIdx.x & (uint32_t)(W - 1);
     const uint32_t L = WordTraits<Word>::count(a.v);
@@ -129,24 +153,54 @@ __global__ void __launch_bounds__(256) k_batch_persistent(BatchArgs a) {
     const unsigned long long warp0 = ((unsigned long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const unsigned long long nwarps = ((unsigned long long)gridDim.x * blockDim.x) >> 5;
     for (unsigned long long chunk = warp0; chunk * 32ull < total; chunk += nwarps) {
-        const unsigned long long q = chunk * 32ull + lane;
+        const unsigned long long q0 = chunk * 32ull;
+        const unsigned long long q = q0 + lane;
         const bool active = q < total;
+        // group of the chunk's first request: one lane searches, the warp shares
+        uint32_t g0 = 0;
+        if (lane == 0) {
+            g0 = find_group_any(pre, a.n_groups, q0, 0u);
+            const unsigned long long nq0 = q0 + nwarps * 32ull;
+            if (nq0 < total) {
+                const uint32_t ng = find_group_any(pre, a.n_groups, nq0, g0);
+                const unsigned long long ns = wrap_slot(groups[ng].offset + (nq0 - pre[ng]), a.arena_len);
+                prefetch_l2(a.arena + ns);
+                prefetch_l2(a.arena + wrap_slot(ns + 31ull, a.arena_len));
+                if (K == BWalk::Collab) {
+                    const uint32_t w0 = idx_hi(lcg31(request_seed(seed, (uint32_t)nq0)), L);
+                    const Word* wp = reinterpret_cast<const Word*>(a.v.words);
+                    prefetch_l2(wp + w0);
+                    prefetch_l2(wp + (w0 + 31u < L ? w0 + 31u : w0 + 31u - L));
+                }
+            }
+        }
+        g0 = __shfl_sync(0xffffffffu, g0, 0);
+        const unsigned long long g0_end = pre[g0 + 1u];
         int op = PBM_OP_ALLOC;
         unsigned long long slot = 0;
         if (active) {
-            // upper_bound over prefix[0..n_groups]
-            uint32_t lo = 0, hi = a.n_groups;   // answer g in [0, n_groups)
-            while (lo + 1u < hi) {
-                uint32_t mid = (lo + hi) >> 1;
-                if (a.prefix[mid] <= q) lo = mid; else hi = mid;
-            }
-            const pbm_group gd = groups[lo];
+            // a chunk usually lies inside one group; lanes past its end search on
+            const uint32_t g = q < g0_end ? g0 : find_group_any(pre, a.n_groups, q, g0);
+            const pbm_group gd = groups[g];
             op = gd.op;
-            slot = (gd.offset + (q - a.prefix[lo])) % a.arena_len;
+            slot = wrap_slot(gd.offset + (q - pre[g]), a.arena_len);
         }
         batch_round<K, W, Word>(a, seed, active, op, q, slot, lane_off, gslots, acc);
     }
     flush_bacc(acc, a.stats);
+    if (a.done) {
+        // every block read the step above; the last one to finish advances it
+        if (threadIdx.x == 0) {
+            __threadfence();
+            s_last = atomicAdd(a.done, 1u) == gridDim.x - 1u;
+        }
+        __syncthreads();
+        if (s_last && threadIdx.x == 0) {
+            *a.done = 0u;
+            *a.d_step = step + 1u;
+            __threadfence();
+        }
+    }
 }
 
 template <BWalk K, int W, typename Word>
@@ -163,77 +217,27 @@ __global__ void __launch_bounds__(256) k_batch_plain(BatchArgs a) {
     for (unsigned long long chunk = warp0; chunk * 32ull < a.count; chunk += nwarps) {
         const unsigned long long ql = chunk * 32ull + lane;
         const bool active = ql < a.count;
-        const unsigned long long slot = (a.offset + ql) % a.arena_len;
+        unsigned long long slot = a.offset + ql;
+        if (slot >= a.arena_len) slot = slot - a.arena_len < a.arena_len ? slot - a.arena_len : slot % a.arena_len;
         batch_round<K, W, Word>(a, a.seed, active, a.op, a.q_base + ql, slot, lane_off, gslots, acc);
     }
     flush_bacc(acc, a.stats);
-}
-
-// Exclusive prefix of the groups' counts (one block of 1024 threads).
-__global__ void k_batch_prefix(const pbm_group* groups, uint32_t n_groups, const uint32_t* d_step,
-                               unsigned long long* prefix) {
-    __shared__ unsigned long long warp_tot[32];
-    __shared__ unsigned long long carry;
-    const uint32_t step = d_step ? *d_step : 0u;
-    const pbm_group* g = groups + (size_t)step * n_groups;
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
-    if (threadIdx.x == 0) carry = 0;
-    __syncthreads();
-    for (uint32_t base = 0; base < n_groups; base += blockDim.x) {
-        uint32_t i = base + threadIdx.x;
-        unsigned long long c = i < n_groups ? (unsigned long long)g[i].count : 0ull;
-        unsigned long long incl = c;
-        for (int d = 1; d < 32; d <<= 1) {
-            unsigned long long y = __shfl_up_sync(0xffffffffu, incl, d);
-            if (lane >= d) incl += y;
-        }
-        if (lane == 31) warp_tot[warp] = incl;
-        __syncthreads();
-        if (warp == 0) {
-            unsigned long long t = lane < nwarps ? warp_tot[lane] : 0ull;
-            unsigned long long ti = t;
-            for (int d = 1; d < 32; d <<= 1) {
-                unsigned long long y = __shfl_up_sync(0xffffffffu, ti, d);
-                if (lane >= d) ti += y;
-            }
-            if (lane < nwarps) warp_tot[lane] = ti - t;   // exclusive warp offsets
-        }
-        __syncthreads();
-        unsigned long long excl = carry + warp_tot[warp] + incl - c;
-        if (i < n_groups) prefix[i] = excl;
-        __syncthreads();
-        if (threadIdx.x == blockDim.x - 1) carry = excl + c;
-        __syncthreads();
-    }
-    if (threadIdx.x == 0) prefix[n_groups] = carry;
-}
-
-__global__ void k_step_advance(uint32_t* d_step) {
-    if (threadIdx.x == 0 && blockIdx.x == 0) *d_step += 1u;
 }
 
 }  // namespace pbm
 
 using namespace pbm;
 
-struct pbm_graph {
-    cudaGraph_t graph;
-    cudaGraphExec_t exec;
-    uint32_t* d_step;
-    unsigned long long* d_prefix;
-    unsigned long long launches_per_replay;
-};
-
 namespace {
 
 // Resident blocks per SM of a persistent instantiation (queried once per block
 // size, outside any stream capture).
-template <BWalk K, int W, typename Word>
+template <BWalk K, int W, typename Word, int MINB>
 int persistent_blocks_per_sm(int block) {
     static int cached_block = 0, cached = 0;
     if (cached_block != block) {
         int n = 0;
-        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_batch_persistent<K, W, Word>, block, 0) !=
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_batch_persistent<K, W, Word, MINB>, block, kFusedPrefixBytes) !=
             cudaSuccess) {
             cudaGetLastError();
             n = 1;
@@ -244,11 +248,21 @@ int persistent_blocks_per_sm(int block) {
     return cached;
 }
 
+// blocks_per_sm <= 0: uncapped registers, as many blocks as fit;
+// 1..5: uncapped registers, that many blocks; >= 6: register-capped variant.
 template <BWalk K, int W, typename Word>
 int launch_batch_kw(const BatchArgs& a, bool persistent, int block, int blocks_per_sm, cudaStream_t s) {
     if (persistent) {
-        int per_sm = blocks_per_sm > 0 ? blocks_per_sm : persistent_blocks_per_sm<K, W, Word>(block);
-        k_batch_persistent<K, W, Word><<<sm_count() * per_sm, block, 0, s>>>(a);
+        const size_t smem = a.fuse ? sizeof(unsigned long long) * (a.n_groups + 1u) : 0u;
+        if (blocks_per_sm >= 6) {
+            int fit = persistent_blocks_per_sm<K, W, Word, 6>(block);
+            int per_sm = blocks_per_sm < fit ? blocks_per_sm : fit;
+            k_batch_persistent<K, W, Word, 6><<<sm_count() * per_sm, block, smem, s>>>(a);
+        } else {
+            int fit = persistent_blocks_per_sm<K, W, Word, 1>(block);
+            int per_sm = (blocks_per_sm > 0 && blocks_per_sm < fit) ? blocks_per_sm : fit;
+            k_batch_persistent<K, W, Word, 1><<<sm_count() * per_sm, block, smem, s>>>(a);
+        }
     } else {
         unsigned long long warps = (a.count + 31ull) / 32ull;
         unsigned long long grid = (warps * 32ull + (unsigned long long)block - 1ull) / (unsigned long long)block;
@@ -283,24 +297,29 @@ int launch_batch(const pbm_walk_config* c, const BatchArgs& a, bool persistent, 
     }
 }
 
+// Blocks per SM the persistent launch of this configuration will use
+// (resolved before a capture, so the capture issues no occupancy query).
 int resolve_blocks_per_sm(const pbm_walk_config* c) {
     const int block = c->block_size ? c->block_size : kDefaultBlock;
     const bool w64 = c->word_bits == 64;
+    const bool capped = c->blocks_per_sm >= 6;
+    auto pick = [&](int fit1, int fit6) {
+        if (capped) return c->blocks_per_sm < fit6 ? c->blocks_per_sm : fit6;
+        return (c->blocks_per_sm > 0 && c->blocks_per_sm < fit1) ? c->blocks_per_sm : fit1;
+    };
+#define PBM_FITS(K, W, T) pick(persistent_blocks_per_sm<K, W, T, 1>(block), persistent_blocks_per_sm<K, W, T, 6>(block))
     switch (c->strategy) {
-    case PBM_RANDOM_WALK: return persistent_blocks_per_sm<BWalk::Page, 32, uint32_t>(block);
+    case PBM_RANDOM_WALK: return PBM_FITS(BWalk::Page, 32, uint32_t);
     case PBM_RANDOM_WALK_BM:
-        return w64 ? persistent_blocks_per_sm<BWalk::Word64, 32, uint64_t>(block)
-                   : persistent_blocks_per_sm<BWalk::Word32, 32, uint32_t>(block);
+        return w64 ? PBM_FITS(BWalk::Word64, 32, uint64_t) : PBM_FITS(BWalk::Word32, 32, uint32_t);
     default: {
         const int W = c->collab_width ? c->collab_width : 32;
-        if (W == 8) return w64 ? persistent_blocks_per_sm<BWalk::Collab, 8, uint64_t>(block)
-                               : persistent_blocks_per_sm<BWalk::Collab, 8, uint32_t>(block);
-        if (W == 16) return w64 ? persistent_blocks_per_sm<BWalk::Collab, 16, uint64_t>(block)
-                                : persistent_blocks_per_sm<BWalk::Collab, 16, uint32_t>(block);
-        return w64 ? persistent_blocks_per_sm<BWalk::Collab, 32, uint64_t>(block)
-                   : persistent_blocks_per_sm<BWalk::Collab, 32, uint32_t>(block);
+        if (W == 8) return w64 ? PBM_FITS(BWalk::Collab, 8, uint64_t) : PBM_FITS(BWalk::Collab, 8, uint32_t);
+        if (W == 16) return w64 ? PBM_FITS(BWalk::Collab, 16, uint64_t) : PBM_FITS(BWalk::Collab, 16, uint32_t);
+        return w64 ? PBM_FITS(BWalk::Collab, 32, uint64_t) : PBM_FITS(BWalk::Collab, 32, uint32_t);
     }
     }
+#undef PBM_FITS
 }
 
 BatchArgs base_args(pbm_pool* p, const pbm_walk_config* c, int32_t* arena, uint64_t arena_len,
@@ -364,6 +383,12 @@ int pbm_batch_launch(pbm_pool* pool, const pbm_walk_config* cfg, const pbm_group
         return PBM_OK;
     }
     if (mode != PBM_LAUNCH_PERSISTENT || !d_groups) return PBM_ERR_INVALID;
+    a.groups = d_groups;
+    a.n_groups = n_groups;
+    if (n_groups <= kFusedGroups) {   // every block scans the groups itself
+        a.fuse = 1;
+        return launch_batch(cfg, a, true, s);
+    }
     if (pool->prefix_cap < n_groups + 1u) {
         cudaFree(pool->d_prefix);
         pool->d_prefix = nullptr;
@@ -394,25 +419,33 @@ int pbm_batch_graph_create(pbm_pool* pool, const pbm_walk_config* cfg, const pbm
     pbm_graph* g = new pbm_graph();
     g->graph = nullptr;
     g->exec = nullptr;
+    g->d_step = nullptr;
+    g->d_done = nullptr;
+    g->d_prefix = nullptr;
     if (cudaMalloc(&g->d_step, sizeof(uint32_t)) != cudaSuccess ||
+        cudaMalloc(&g->d_done, sizeof(uint32_t)) != cudaSuccess ||
         cudaMalloc(&g->d_prefix, sizeof(unsigned long long) * (n_groups + 1u)) != cudaSuccess) {
         cudaGetLastError();
         cudaFree(g->d_step);
+        cudaFree(g->d_done);
         delete g;
         return PBM_ERR_NOMEM;
     }
     PBM_CUDA_TRY(cudaMemsetAsync(g->d_step, 0, sizeof(uint32_t), s));
+    PBM_CUDA_TRY(cudaMemsetAsync(g->d_done, 0, sizeof(uint32_t), s));
     PBM_CUDA_TRY(cudaStreamSynchronize(s));
     BatchArgs a = base_args(pool, cfg, d_arena, arena_len, seed0, nullptr);
     a.groups = d_groups;
     a.n_groups = n_groups;
     a.prefix = g->d_prefix;
     a.d_step = g->d_step;
+    a.done = g->d_done;                       // the last block advances the step
+    a.fuse = n_groups <= kFusedGroups ? 1 : 0;
     // Capture on a private stream (the legacy default stream cannot be
     // captured); the graph is replayed later on the caller's stream.  The
     // occupancy query runs before capture.
     pbm_walk_config c2 = *cfg;
-    if (c2.blocks_per_sm <= 0) c2.blocks_per_sm = resolve_blocks_per_sm(cfg);
+    resolve_blocks_per_sm(cfg);   // fills the occupancy caches before the capture starts
     cudaStream_t cap = nullptr;
     PBM_CUDA_TRY(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
     const unsigned long long before = g_launches.load();
@@ -425,11 +458,11 @@ int pbm_batch_graph_create(pbm_pool* pool, const pbm_walk_config* cfg, const pbm
         delete g;
         return PBM_ERR_CUDA;
     }
-    k_batch_prefix<<<1, 1024, 0, cap>>>(d_groups, n_groups, g->d_step, g->d_prefix);
-    count_launch();
+    if (!a.fuse) {
+        k_batch_prefix<<<1, 1024, 0, cap>>>(d_groups, n_groups, g->d_step, g->d_prefix);
+        count_launch();
+    }
     rc = launch_batch(&c2, a, true, cap);
-    k_step_advance<<<1, 32, 0, cap>>>(g->d_step);
-    count_launch();
     cudaGraph_t graph = nullptr;
     e = cudaStreamEndCapture(cap, &graph);
     cudaStreamDestroy(cap);
@@ -477,6 +510,7 @@ int pbm_graph_destroy(pbm_graph* g) {
     if (g->exec) cudaGraphExecDestroy(g->exec);
     if (g->graph) cudaGraphDestroy(g->graph);
     cudaFree(g->d_step);
+    cudaFree(g->d_done);
     cudaFree(g->d_prefix);
     delete g;
     return PBM_OK;

@@ -218,6 +218,18 @@ __global__ void k_bm_check(BmView b, BmCheck* out) {
     if (pins) atomicAdd(&out->pins, pins);
 }
 
+__global__ void k_bm_gather(BmView b, const int32_t* ids, uint32_t n, uint32_t words_per_frame, int32_t* out) {
+    const unsigned long long total = (unsigned long long)n * words_per_frame;
+    for (unsigned long long i = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; i < total;
+         i += (unsigned long long)gridDim.x * blockDim.x) {
+        uint32_t r = (uint32_t)(i / words_per_frame), k = (uint32_t)(i % words_per_frame);
+        int32_t f = ids[r];
+        out[i] = (f >= 0 && (uint32_t)f < b.n_frames)
+                     ? reinterpret_cast<const int32_t*>(b.frames + (size_t)(uint32_t)f * b.frame_size)[k]
+                     : 0;
+    }
+}
+
 }  // namespace
 }  // namespace pbm
 
@@ -340,6 +352,18 @@ int pbm_bufmgr_check(pbm_bufmgr* m, pbm_bufmgr_check_result* h_out, void* stream
     h_out->loading = c.loading;
     h_out->pins = c.pins;
     return (c.mismatches || c.loading || c.resident != c.mapped_frames) ? PBM_ERR_CORRUPT : PBM_OK;
+}
+
+int pbm_bufmgr_gather(pbm_bufmgr* m, const int32_t* d_frame_ids, uint32_t n, uint32_t bytes_per_frame,
+                      int32_t* d_out, void* stream) {
+    if (!m || !m->v.frames || (n && (!d_frame_ids || !d_out)) || bytes_per_frame == 0 ||
+        bytes_per_frame > m->v.frame_size || (bytes_per_frame & 3u))
+        return PBM_ERR_INVALID;
+    if (n == 0) return PBM_OK;
+    k_bm_gather<<<sm_count() * 4, 256, 0, (cudaStream_t)stream>>>(m->v, d_frame_ids, n, bytes_per_frame / 4u,
+                                                                  d_out);
+    PBM_LAUNCH_CHECK();
+    return PBM_OK;
 }
 
 int pbm_bufmgr_frames(pbm_bufmgr* m, void** d_frames, size_t* bytes) {

@@ -1,0 +1,379 @@
+// malloc.cu -- batched size-classed malloc / free (pbm/pbm_malloc.cuh) over a
+// pool's pages: plain (one launch per group), persistent (one launch), a
+// one-warp deterministic replay, and the CUDA-graph form.
+//
+// Reference: mallocRW / freeRW (source/RWMalloc.cuh:299-334), the
+// KernelMallocCollab allocator (source/malloc.cu:223-320) and the
+// malloc/free drivers (unitTests/unitTest3.cu, unitTestMalloc1.cu).
+#include <new>
+
+#include "batch_common.cuh"
+#include "pbm/pbm_malloc.cuh"
+
+namespace pbm {
+namespace {
+
+struct MArgs {
+    MallocView m;
+    const pbm_group* groups;
+    uint32_t n_groups;
+    const uint32_t* d_step;
+    uint32_t seed;
+    const uint32_t* sizes;            // per slot
+    unsigned long long* ptrs;         // per slot (device addresses, 0 = none)
+    unsigned long long arena_len;
+    const unsigned long long* prefix;
+    uint32_t max_steps;
+    DevStats* stats;
+    int32_t op;                       // plain form: the one group this launch serves
+    uint32_t count;
+    unsigned long long offset;
+    unsigned long long q_base;
+};
+
+struct MAcc {
+    unsigned long long ok = 0, fail = 0, steps = 0, frees = 0, bad = 0;
+};
+
+__device__ __forceinline__ unsigned long long wrap(unsigned long long slot, unsigned long long len) {
+    if (slot >= len) slot = slot - len < len ? slot - len : slot % len;
+    return slot;
+}
+
+template <bool SERIAL>
+__device__ __forceinline__ void malloc_round(const MArgs& a, uint32_t seed, bool active, int op,
+                                             unsigned long long q0, unsigned long long q,
+                                             unsigned long long slot, MAcc& acc) {
+    const bool do_malloc = active && op == PBM_OP_MALLOC;
+    const bool do_free = active && op == PBM_OP_MFREE;
+    const uint64_t size = do_malloc ? (uint64_t)a.sizes[slot] : 0ull;
+    int32_t s = 0;
+    void* p = malloc_group(a.m, 0xffffffffu, size, request_seed(seed ^ 0x9E3779B9u, (uint32_t)q0),
+                           request_seed(seed, (uint32_t)q), a.max_steps, SERIAL, &s);
+    if (do_malloc) {
+        a.ptrs[slot] = (unsigned long long)p;
+        if (size) {
+            acc.ok += p != nullptr;
+            acc.fail += p == nullptr;
+            acc.steps += (unsigned long long)s;
+        }
+    }
+    const void* fp = do_free ? (const void*)a.ptrs[slot] : nullptr;
+    const bool ok = free_group(a.m, 0xffffffffu, fp);
+    if (do_free) {
+        a.ptrs[slot] = 0ull;
+        if (fp) {
+            acc.frees += ok;
+            acc.bad += !ok;
+        }
+    }
+}
+
+__device__ __forceinline__ void flush_macc(const MAcc& c, DevStats* st) {
+    if (c.ok) atomicAdd(&st->successes, c.ok);
+    if (c.fail) atomicAdd(&st->failures, c.fail);
+    if (c.steps) atomicAdd(&st->steps, c.steps);
+    if (c.frees) atomicAdd(&st->frees, c.frees);
+    if (c.bad) atomicAdd(&st->bad_frees, c.bad);
+}
+
+template <bool SERIAL>
+__global__ void __launch_bounds__(256) k_malloc_persistent(MArgs a) {
+    MAcc acc;
+    const uint32_t step = a.d_step ? *a.d_step : 0u;
+    const pbm_group* groups = a.groups + (size_t)step * a.n_groups;
+    const uint32_t seed = a.seed + step;
+    const unsigned long long total = a.prefix[a.n_groups];
+    const uint32_t lane = threadIdx.x & 31u;
+    const unsigned long long warp0 = ((unsigned long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const unsigned long long nwarps = ((unsigned long long)gridDim.x * blockDim.x) >> 5;
+    for (unsigned long long chunk = warp0; chunk * 32ull < total; chunk += nwarps) {
+        const unsigned long long q0 = chunk * 32ull;
+        const unsigned long long q = q0 + lane;
+        const bool active = q < total;
+        uint32_t g0 = 0;
+        if (lane == 0) g0 = find_group(a.prefix, a.n_groups, q0, 0u);
+        g0 = __shfl_sync(0xffffffffu, g0, 0);
+        const unsigned long long g0_end = __ldg(a.prefix + g0 + 1u);
+        int op = PBM_OP_MALLOC;
+        unsigned long long slot = 0;
+        if (active) {
+            const uint32_t g = q < g0_end ? g0 : find_group(a.prefix, a.n_groups, q, g0);
+            const pbm_group gd = groups[g];
+            op = gd.op;
+            slot = wrap(gd.offset + (q - __ldg(a.prefix + g)), a.arena_len);
+        }
+        malloc_round<SERIAL>(a, seed, active, op, q0, q, slot, acc);
+    }
+    flush_macc(acc, a.stats);
+}
+
+__global__ void __launch_bounds__(256) k_malloc_plain(MArgs a) {
+    MAcc acc;
+    const uint32_t lane = threadIdx.x & 31u;
+    const unsigned long long warp0 = ((unsigned long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const unsigned long long nwarps = ((unsigned long long)gridDim.x * blockDim.x) >> 5;
+    for (unsigned long long chunk = warp0; chunk * 32ull < a.count; chunk += nwarps) {
+        const unsigned long long ql = chunk * 32ull + lane;
+        const bool active = ql < a.count;
+        malloc_round<false>(a, a.seed, active, a.op, a.q_base + chunk * 32ull, a.q_base + ql,
+                            wrap(a.offset + ql, a.arena_len), acc);
+    }
+    flush_macc(acc, a.stats);
+}
+
+__global__ void k_malloc_init(int32_t* start_of, int32_t* live, uint8_t* len_of, uint32_t n) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        start_of[i] = -1;
+        live[i] = 0;
+        len_of[i] = 0;
+    }
+}
+
+struct MallocTables {
+    int32_t* start_of = nullptr;
+    int32_t* live = nullptr;
+    uint8_t* len_of = nullptr;
+    unsigned long long* prefix = nullptr;
+    uint32_t prefix_cap = 0;
+};
+
+}  // namespace
+}  // namespace pbm
+
+using namespace pbm;
+
+namespace {
+
+// Malloc tables of a pool live beside it, keyed by the pool handle.
+struct Registry {
+    pbm_pool* pool;
+    MallocTables t;
+};
+Registry g_reg[64];
+int g_nreg = 0;
+
+MallocTables* tables_of(pbm_pool* p) {
+    for (int i = 0; i < g_nreg; ++i) if (g_reg[i].pool == p) return &g_reg[i].t;
+    return nullptr;
+}
+
+MallocView view_of(pbm_pool* p, const MallocTables* t) {
+    MallocView m;
+    m.pool = p->view;
+    m.start_of = t->start_of;
+    m.live = t->live;
+    m.len_of = t->len_of;
+    uint32_t sh = 0;
+    while ((1u << sh) < p->page_size) ++sh;
+    m.page_shift = sh;
+    return m;
+}
+
+int check_pool(pbm_pool* p) {
+    if (!p || !p->d_base) return PBM_ERR_INVALID;
+    if ((p->page_size & (p->page_size - 1u)) || p->page_size < 2048u || p->page_size > (1u << 16))
+        return PBM_ERR_INVALID;
+    return PBM_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int pbm_malloc_init(pbm_pool* pool) {
+    int rc = check_pool(pool);
+    if (rc) return rc;
+    if (tables_of(pool)) return PBM_OK;
+    if (g_nreg >= 64) return PBM_ERR_NOMEM;
+    MallocTables t;
+    const size_t n = pool->n_pages;
+    if (cudaMalloc(&t.start_of, n * 4) != cudaSuccess || cudaMalloc(&t.live, n * 4) != cudaSuccess ||
+        cudaMalloc(&t.len_of, n) != cudaSuccess) {
+        cudaGetLastError();
+        cudaFree(t.start_of);
+        cudaFree(t.live);
+        return PBM_ERR_NOMEM;
+    }
+    k_malloc_init<<<sm_count() * 4, 256>>>(t.start_of, t.live, t.len_of, (uint32_t)n);
+    PBM_LAUNCH_CHECK();
+    PBM_CUDA_TRY(cudaDeviceSynchronize());
+    g_reg[g_nreg].pool = pool;
+    g_reg[g_nreg].t = t;
+    ++g_nreg;
+    return PBM_OK;
+}
+
+int pbm_malloc_tables(pbm_pool* pool, void** d_start_of, void** d_live, void** d_len_of) {
+    MallocTables* t = tables_of(pool);
+    if (!t) return PBM_ERR_INVALID;
+    if (d_start_of) *d_start_of = t->start_of;
+    if (d_live) *d_live = t->live;
+    if (d_len_of) *d_len_of = t->len_of;
+    return PBM_OK;
+}
+
+int pbm_malloc_release(pbm_pool* pool) {
+    for (int i = 0; i < g_nreg; ++i) {
+        if (g_reg[i].pool != pool) continue;
+        cudaDeviceSynchronize();
+        cudaFree(g_reg[i].t.start_of);
+        cudaFree(g_reg[i].t.live);
+        cudaFree(g_reg[i].t.len_of);
+        cudaFree(g_reg[i].t.prefix);
+        g_reg[i] = g_reg[--g_nreg];
+        return PBM_OK;
+    }
+    return PBM_ERR_INVALID;
+}
+
+int pbm_malloc_batch(pbm_pool* pool, const pbm_group* d_groups, const pbm_group* h_groups, uint32_t n_groups,
+                     const uint32_t* d_sizes, unsigned long long* d_ptrs, uint64_t arena_len, uint32_t seed,
+                     uint32_t max_steps, int mode, void* stream) {
+    MallocTables* t = tables_of(pool);
+    if (!t || !d_ptrs || !arena_len) return PBM_ERR_INVALID;
+    if (n_groups == 0) return PBM_OK;
+    cudaStream_t s = (cudaStream_t)stream;
+    pool->fifo_valid = false;
+    MArgs a{};
+    a.m = view_of(pool, t);
+    a.seed = seed;
+    a.sizes = d_sizes;
+    a.ptrs = d_ptrs;
+    a.arena_len = arena_len;
+    a.max_steps = max_steps ? max_steps : kDefaultMaxSteps;
+    a.stats = pool->d_stats;
+    if (mode == PBM_LAUNCH_PLAIN) {
+        if (!h_groups) return PBM_ERR_INVALID;
+        unsigned long long q = 0;
+        for (uint32_t g = 0; g < n_groups; ++g) {
+            const pbm_group& gd = h_groups[g];
+            if (gd.op != PBM_OP_MALLOC && gd.op != PBM_OP_MFREE) return PBM_ERR_INVALID;
+            if (gd.count == 0) continue;
+            a.op = gd.op;
+            a.count = gd.count;
+            a.offset = gd.offset;
+            a.q_base = q;
+            const unsigned long long warps = (gd.count + 31ull) / 32ull;
+            const unsigned grid = (unsigned)((warps * 32ull + 255ull) / 256ull);
+            k_malloc_plain<<<grid, 256, 0, s>>>(a);
+            PBM_LAUNCH_CHECK();
+            q += gd.count;
+        }
+        return PBM_OK;
+    }
+    if ((mode != PBM_LAUNCH_PERSISTENT && mode != PBM_LAUNCH_SERIAL) || !d_groups) return PBM_ERR_INVALID;
+    if (t->prefix_cap < n_groups + 1u) {
+        cudaFree(t->prefix);
+        t->prefix = nullptr;
+        if (cudaMalloc(&t->prefix, sizeof(unsigned long long) * (n_groups + 1u)) != cudaSuccess) {
+            cudaGetLastError();
+            t->prefix_cap = 0;
+            return PBM_ERR_NOMEM;
+        }
+        t->prefix_cap = n_groups + 1u;
+    }
+    k_batch_prefix<<<1, 1024, 0, s>>>(d_groups, n_groups, nullptr, t->prefix);
+    PBM_LAUNCH_CHECK();
+    a.groups = d_groups;
+    a.n_groups = n_groups;
+    a.prefix = t->prefix;
+    if (mode == PBM_LAUNCH_SERIAL) {
+        k_malloc_persistent<true><<<1, 32, 0, s>>>(a);
+    } else {
+        int per_sm = 0;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_malloc_persistent<false>, 256, 0);
+        if (per_sm < 1) per_sm = 1;
+        k_malloc_persistent<false><<<sm_count() * per_sm, 256, 0, s>>>(a);
+    }
+    PBM_LAUNCH_CHECK();
+    return PBM_OK;
+}
+
+int pbm_malloc_graph_create(pbm_pool* pool, const pbm_group* d_groups, uint32_t n_groups, uint32_t n_steps,
+                            const uint32_t* d_sizes, unsigned long long* d_ptrs, uint64_t arena_len,
+                            uint32_t seed0, uint32_t max_steps, void* stream, pbm_graph** out) {
+    MallocTables* t = tables_of(pool);
+    if (!t || !d_groups || !d_ptrs || !out || !n_groups || !n_steps || !arena_len) return PBM_ERR_INVALID;
+    *out = nullptr;
+    cudaStream_t s = (cudaStream_t)stream;
+    pbm_graph* g = new pbm_graph();
+    g->graph = nullptr;
+    g->exec = nullptr;
+    if (cudaMalloc(&g->d_step, sizeof(uint32_t)) != cudaSuccess ||
+        cudaMalloc(&g->d_prefix, sizeof(unsigned long long) * (n_groups + 1u)) != cudaSuccess) {
+        cudaGetLastError();
+        cudaFree(g->d_step);
+        delete g;
+        return PBM_ERR_NOMEM;
+    }
+    PBM_CUDA_TRY(cudaMemsetAsync(g->d_step, 0, sizeof(uint32_t), s));
+    PBM_CUDA_TRY(cudaStreamSynchronize(s));
+    MArgs a{};
+    a.m = view_of(pool, t);
+    a.groups = d_groups;
+    a.n_groups = n_groups;
+    a.d_step = g->d_step;
+    a.seed = seed0;
+    a.sizes = d_sizes;
+    a.ptrs = d_ptrs;
+    a.arena_len = arena_len;
+    a.prefix = g->d_prefix;
+    a.max_steps = max_steps ? max_steps : kDefaultMaxSteps;
+    a.stats = pool->d_stats;
+    int per_sm = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_malloc_persistent<false>, 256, 0);
+    if (per_sm < 1) per_sm = 1;
+    cudaStream_t cap = nullptr;
+    PBM_CUDA_TRY(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
+    cudaError_t e = cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal);
+    if (e == cudaSuccess) {
+        k_batch_prefix<<<1, 1024, 0, cap>>>(d_groups, n_groups, g->d_step, g->d_prefix);
+        k_malloc_persistent<false><<<sm_count() * per_sm, 256, 0, cap>>>(a);
+        k_step_advance<<<1, 32, 0, cap>>>(g->d_step);
+        cudaGraph_t graph = nullptr;
+        e = cudaStreamEndCapture(cap, &graph);
+        if (e == cudaSuccess) {
+            g->graph = graph;
+            e = cudaGraphInstantiate(&g->exec, graph, 0);
+        }
+    }
+    cudaStreamDestroy(cap);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        if (g->graph) cudaGraphDestroy(g->graph);
+        cudaFree(g->d_step);
+        cudaFree(g->d_prefix);
+        delete g;
+        return PBM_ERR_CUDA;
+    }
+    g->launches_per_replay = 3;
+    pool->fifo_valid = false;
+    *out = g;
+    return PBM_OK;
+}
+
+int pbm_malloc_counts(pbm_pool* pool, uint64_t* h_live_runs, uint64_t* h_bad_frees, void* stream) {
+    MallocTables* t = tables_of(pool);
+    if (!t) return PBM_ERR_INVALID;
+    cudaStream_t s = (cudaStream_t)stream;
+    DevStats d;
+    PBM_CUDA_TRY(cudaMemcpyAsync(&d, pool->d_stats, sizeof(d), cudaMemcpyDeviceToHost, s));
+    PBM_CUDA_TRY(cudaStreamSynchronize(s));
+    if (h_bad_frees) *h_bad_frees = d.bad_frees;
+    if (h_live_runs) {
+        // runs still holding blocks: count first pages with live > 0 (host scan of a snapshot)
+        const size_t n = pool->n_pages;
+        int32_t* h = new (std::nothrow) int32_t[n];
+        if (!h) return PBM_ERR_NOMEM;
+        cudaError_t e = cudaMemcpy(h, t->live, n * 4, cudaMemcpyDeviceToHost);
+        uint64_t c = 0;
+        for (size_t i = 0; i < n; ++i) c += h[i] > 0;
+        delete[] h;
+        if (e != cudaSuccess) { cudaGetLastError(); return PBM_ERR_CUDA; }
+        *h_live_runs = c;
+    }
+    return PBM_OK;
+}
+
+}  // extern "C"

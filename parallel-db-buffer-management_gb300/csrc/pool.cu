@@ -325,6 +325,7 @@ int pbm_pool_create(const pbm_pool_config* cfg, pbm_pool** out) {
 int pbm_pool_destroy(pbm_pool* pool) {
     if (!pool) return PBM_ERR_INVALID;
     cudaDeviceSynchronize();
+    pbm_malloc_release(pool);   // malloc side tables, if any
     pool_free_all(pool);
     return PBM_OK;
 }

@@ -42,8 +42,8 @@ STRATEGY_NAMES = {
     SINGLE_CLOCK: "SingleClock", DIST_CLOCK: "DistClock",
 }
 
-OP_ALLOC, OP_FREE, OP_SWAP = 0, 1, 2
-LAUNCH_PLAIN, LAUNCH_PERSISTENT = 0, 1
+OP_ALLOC, OP_FREE, OP_SWAP, OP_MALLOC, OP_MFREE = 0, 1, 2, 3, 4
+LAUNCH_PLAIN, LAUNCH_PERSISTENT, LAUNCH_SERIAL = 0, 1, 2
 POOL_MATERIALIZE = 1
 
 
@@ -82,6 +82,11 @@ class DeviceState(Structure):
 BM_SINGLE_CLOCK, BM_DIST_CLOCK = 0, 1
 
 
+class TuneResult(Structure):
+    _fields_ = [("cfg", WalkConfig), ("ms_per_batch", ctypes.c_float), ("reserved", ctypes.c_float),
+                ("ops_per_s", c_double)]
+
+
 class BufMgrConfig(Structure):
     _fields_ = [("n_logical", c_uint64), ("n_frames", c_uint32), ("frame_size", c_uint32),
                 ("policy", c_int32), ("n_arms", c_uint32), ("max_sweep", c_uint32), ("reserved", c_uint32)]
@@ -95,6 +100,31 @@ class BufMgrCounters(Structure):
 class BufMgrCheck(Structure):
     _fields_ = [("resident", c_uint64), ("mapped_frames", c_uint64), ("mismatches", c_uint64),
                 ("loading", c_uint64), ("pins", c_uint64)]
+
+
+REQ_ALLOC, REQ_FREE, REQ_FETCH = 0, 1, 2
+
+
+class Request(Structure):
+    _fields_ = [("arrival_s", c_double), ("tenant", c_uint32), ("op", c_int32), ("count", c_uint32),
+                ("reserved", c_uint32)]
+
+
+class RequestResult(Structure):
+    _fields_ = [("admit_s", c_double), ("launch_s", c_double), ("done_s", c_double), ("latency_s", c_double),
+                ("pages", c_uint64), ("status", c_int32), ("reserved", c_uint32)]
+
+
+class ServerConfig(Structure):
+    _fields_ = [("n_tenants", c_uint32), ("ring_pages", c_uint32), ("n_streams", c_uint32),
+                ("max_batch_requests", c_uint32), ("max_fetch_pages", c_uint32), ("reserved", c_uint32),
+                ("max_occupancy", c_double), ("drain_timeout_s", c_double), ("walk", WalkConfig)]
+
+
+class ServerReport(Structure):
+    _fields_ = [("requests", c_uint64), ("completed", c_uint64), ("rejected", c_uint64), ("pages", c_uint64),
+                ("batches", c_uint64), ("max_in_flight", c_uint64), ("wall_s", c_double), ("p50_s", c_double),
+                ("p99_s", c_double), ("mean_batch_requests", c_double)]
 
 
 # (name, restype, argtypes) -- every entry point of include/pbm.h
@@ -134,6 +164,16 @@ SIGNATURES = [
                                       c_void_p]),
     ("pbm_atomic_ceiling", c_int, [c_uint32, c_uint32, c_uint32, c_int, c_int, POINTER(c_double),
                                    POINTER(c_double)]),
+    ("pbm_malloc_init", c_int, [c_void_p]),
+    ("pbm_malloc_release", c_int, [c_void_p]),
+    ("pbm_malloc_tables", c_int, [c_void_p, POINTER(c_void_p), POINTER(c_void_p), POINTER(c_void_p)]),
+    ("pbm_malloc_batch", c_int, [c_void_p, c_void_p, POINTER(Group), c_uint32, c_void_p, c_void_p, c_uint64,
+                                 c_uint32, c_uint32, c_int, c_void_p]),
+    ("pbm_malloc_graph_create", c_int, [c_void_p, c_void_p, c_uint32, c_uint32, c_void_p, c_void_p, c_uint64,
+                                        c_uint32, c_uint32, c_void_p, POINTER(c_void_p)]),
+    ("pbm_malloc_counts", c_int, [c_void_p, POINTER(c_uint64), POINTER(c_uint64), c_void_p]),
+    ("pbm_autotune", c_int, [c_void_p, c_void_p, c_uint32, c_uint64, c_void_p, c_uint64, c_uint32, c_int,
+                             c_uint32, POINTER(TuneResult), c_uint32, POINTER(c_uint32), c_void_p]),
     ("pbm_bufmgr_create", c_int, [POINTER(BufMgrConfig), c_void_p, POINTER(c_void_p)]),
     ("pbm_bufmgr_destroy", c_int, [c_void_p]),
     ("pbm_bufmgr_reset", c_int, [c_void_p, c_void_p]),
@@ -142,6 +182,12 @@ SIGNATURES = [
     ("pbm_bufmgr_stats", c_int, [c_void_p, POINTER(BufMgrCounters), c_void_p]),
     ("pbm_bufmgr_check", c_int, [c_void_p, POINTER(BufMgrCheck), c_void_p]),
     ("pbm_bufmgr_frames", c_int, [c_void_p, POINTER(c_void_p), POINTER(c_size_t)]),
+    ("pbm_bufmgr_gather", c_int, [c_void_p, c_void_p, c_uint32, c_uint32, c_void_p, c_void_p]),
+    ("pbm_server_create", c_int, [c_void_p, c_void_p, c_void_p, c_uint64, POINTER(ServerConfig),
+                                  POINTER(c_void_p)]),
+    ("pbm_server_run", c_int, [c_void_p, POINTER(Request), c_uint64, POINTER(RequestResult), POINTER(ServerReport)]),
+    ("pbm_server_tenant_pages", c_int, [c_void_p, c_uint32, c_void_p, c_uint64, POINTER(c_uint64)]),
+    ("pbm_server_destroy", c_int, [c_void_p]),
     ("pbm_version", c_char_p, []),
     ("pbm_kernel_launches", c_uint64, []),
     ("pbm_device_sm_count", c_int, [POINTER(c_int)]),
@@ -308,6 +354,38 @@ class Pool:
                                                _ptr(arena), arena_len, seed0, stream, byref(g)))
         return Graph(self.lib, g)
 
+    # size-classed malloc -----------------------------------------------------------
+    def malloc_init(self):
+        _check("pbm_malloc_init", self.lib.pbm_malloc_init(self.h))
+
+    def malloc_batch(self, d_groups, h_groups, n_groups, sizes, ptrs, arena_len, seed, mode, max_steps=4096,
+                     stream=0):
+        return _check("pbm_malloc_batch",
+                      self.lib.pbm_malloc_batch(self.h, _ptr(d_groups), h_groups, n_groups, _ptr(sizes), _ptr(ptrs),
+                                                arena_len, seed, max_steps, mode, stream))
+
+    def malloc_graph(self, d_groups, n_groups, n_steps, sizes, ptrs, arena_len, seed0, max_steps=4096, stream=0):
+        g = c_void_p()
+        _check("pbm_malloc_graph_create",
+               self.lib.pbm_malloc_graph_create(self.h, _ptr(d_groups), n_groups, n_steps, _ptr(sizes), _ptr(ptrs),
+                                                arena_len, seed0, max_steps, stream, byref(g)))
+        return Graph(self.lib, g)
+
+    def malloc_counts(self, stream=0):
+        live, bad = c_uint64(), c_uint64()
+        _check("pbm_malloc_counts", self.lib.pbm_malloc_counts(self.h, byref(live), byref(bad), stream))
+        return live.value, bad.value
+
+    def autotune(self, d_groups, n_groups, requests, arena, arena_len, seed=77, reps=3, max_steps=4096,
+                 max_out=64, stream=0):
+        """Candidate configurations for this pool's occupancy, fastest first."""
+        out = (TuneResult * max_out)()
+        n = c_uint32()
+        _check("pbm_autotune", self.lib.pbm_autotune(self.h, _ptr(d_groups), n_groups, requests, _ptr(arena),
+                                                     arena_len, seed, reps, max_steps, out, max_out, byref(n),
+                                                     stream))
+        return [out[i] for i in range(n.value)]
+
     def check(self, ids, n, stream=0) -> CheckResult:
         r = CheckResult()
         rc = self.lib.pbm_check_ids(self.h, _ptr(ids), n, byref(r), stream)
@@ -367,6 +445,10 @@ class BufferManager:
         _check("pbm_bufmgr_check", self.lib.pbm_bufmgr_check(self.h, byref(c), stream), allow=(ERR_CORRUPT,))
         return c
 
+    def gather(self, frame_ids, n, bytes_per_frame, out, stream=0):
+        return _check("pbm_bufmgr_gather", self.lib.pbm_bufmgr_gather(self.h, _ptr(frame_ids), n, bytes_per_frame,
+                                                                      _ptr(out), stream))
+
     def frames(self):
         p, n = c_void_p(), c_size_t()
         _check("pbm_bufmgr_frames", self.lib.pbm_bufmgr_frames(self.h, byref(p), byref(n)))
@@ -375,6 +457,55 @@ class BufferManager:
     def close(self):
         if self.h:
             self.lib.pbm_bufmgr_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Server:
+    """Continuous-batching serving loop over a pool (and optional buffer manager)."""
+
+    def __init__(self, pool: Pool, n_tenants, ring_pages, n_streams=4, max_batch_requests=1024,
+                 max_occupancy=0.95, drain_timeout_s=2.0, walk=None, bufmgr=None, fetch_pages=None,
+                 max_fetch_pages=0):
+        self.lib = lib()
+        cfg = ServerConfig(n_tenants, ring_pages, n_streams, max_batch_requests, max_fetch_pages, 0,
+                           max_occupancy, drain_timeout_s, walk or walk_config())
+        h = c_void_p()
+        nf = 0 if fetch_pages is None else fetch_pages.numel()
+        _check("pbm_server_create", self.lib.pbm_server_create(pool.h, bufmgr.h if bufmgr else None,
+                                                               _ptr(fetch_pages), nf, byref(cfg), byref(h)))
+        self.h = h
+        self.n_tenants = n_tenants
+
+    def run(self, arrivals, tenants, ops, counts):
+        n = len(arrivals)
+        reqs = (Request * n)()
+        for i in range(n):
+            reqs[i] = Request(float(arrivals[i]), int(tenants[i]), int(ops[i]), int(counts[i]), 0)
+        res = (RequestResult * n)()
+        rep = ServerReport()
+        rc = self.lib.pbm_server_run(self.h, reqs, n, res, byref(rep))
+        _check("pbm_server_run", rc, allow=(ERR_TIMEOUT,))
+        return res, rep, rc
+
+    def tenant_pages(self, tenant):
+        import numpy as np
+
+        k = c_uint64()
+        _check("pbm_server_tenant_pages", self.lib.pbm_server_tenant_pages(self.h, tenant, None, 0, byref(k)))
+        out = np.empty(k.value, dtype=np.int32)
+        _check("pbm_server_tenant_pages",
+               self.lib.pbm_server_tenant_pages(self.h, tenant, out.ctypes.data, k.value, byref(k)))
+        return out
+
+    def close(self):
+        if self.h:
+            self.lib.pbm_server_destroy(self.h)
             self.h = None
 
     def __del__(self):

@@ -69,3 +69,65 @@ extern "C" int dropin_run(int nGB, int pageSize, float prefillFree, int n, int b
     cudaFree(d_bad);
     return cudaGetLastError() == cudaSuccess ? 0 : -2;
 }
+
+#ifdef PBM_WITH_MALLOC
+// mallocRW / freeRW from a caller's kernels (unitTests/unitTest3.cu shape):
+// every thread takes a block, fills it with its id, and frees it later.
+__global__ void malloc_kernel(int n, const int* sizes, unsigned long long* ptrs) {
+    int tid = blockIdx.x * blockDim.x + threadIdx.x;
+    if (tid < n) {
+        void* p = mallocRW((size_t)sizes[tid]);
+        ptrs[tid] = (unsigned long long)p;
+        if (p) {
+            int* q = (int*)p;
+            for (int k = 0; k < sizes[tid] / 4; ++k) q[k] = tid;
+        }
+    }
+}
+
+__global__ void malloc_check(int n, const int* sizes, const unsigned long long* ptrs, int* bad) {
+    int tid = blockIdx.x * blockDim.x + threadIdx.x;
+    if (tid < n) {
+        const int* q = (const int*)ptrs[tid];
+        if (!q) { atomicAdd(bad, 1); return; }
+        for (int k = 0; k < sizes[tid] / 4; ++k)
+            if (q[k] != tid) { atomicAdd(bad, 1); return; }
+    }
+}
+
+__global__ void mfree_kernel(int n, const unsigned long long* ptrs) {
+    int tid = blockIdx.x * blockDim.x + threadIdx.x;
+    if (tid < n) freeRW((void*)ptrs[tid]);
+}
+
+// out: [0] failed or overwritten blocks, [1] free fraction before (x1e6),
+// [2] after malloc, [3] after free
+extern "C" int dropin_malloc_run(int nGB, int pageSize, int n, const int* h_sizes, long long* out) {
+    initMemoryManagement(nGB, pageSize);
+    int *d_sizes = nullptr, *d_bad = nullptr;
+    unsigned long long* d_ptrs = nullptr;
+    cudaMalloc(&d_sizes, n * sizeof(int));
+    cudaMalloc(&d_ptrs, n * sizeof(unsigned long long));
+    cudaMalloc(&d_bad, sizeof(int));
+    cudaMemcpy(d_sizes, h_sizes, n * sizeof(int), cudaMemcpyHostToDevice);
+    cudaMemset(d_bad, 0, sizeof(int));
+    float f0 = getFreePagePercentage();
+    malloc_kernel<<<(n + 63) / 64, 64>>>(n, d_sizes, d_ptrs);
+    malloc_check<<<(n + 255) / 256, 256>>>(n, d_sizes, d_ptrs, d_bad);
+    cudaDeviceSynchronize();
+    float f1 = getFreePagePercentage();
+    mfree_kernel<<<(n + 63) / 64, 64>>>(n, d_ptrs);
+    cudaDeviceSynchronize();
+    float f2 = getFreePagePercentage();
+    int bad = 0;
+    cudaMemcpy(&bad, d_bad, sizeof(int), cudaMemcpyDeviceToHost);
+    out[0] = bad;
+    out[1] = (long long)(f0 * 1e6 + 0.5);
+    out[2] = (long long)(f1 * 1e6 + 0.5);
+    out[3] = (long long)(f2 * 1e6 + 0.5);
+    cudaFree(d_sizes);
+    cudaFree(d_ptrs);
+    cudaFree(d_bad);
+    return cudaGetLastError() == cudaSuccess ? 0 : -2;
+}
+#endif

@@ -54,3 +54,93 @@ def test_reference_style_driver(cuda, callers, family, n, block):
     assert f2 == f0                                    # freed exactly those pages
     assert f3 == 1_000_000                             # resetMemoryManager()
     assert ssum >= n
+
+
+def test_rwmalloc_dropin_blocks_are_private_and_released(cuda, pbm_mod):
+    """mallocRW / freeRW from a caller's kernels: every block is filled with
+    its owner's id and read back intact (no overlap), and freeRW of every
+    block returns the pool to its starting occupancy."""
+    import numpy as np
+
+    os.makedirs(BUILD, exist_ok=True)
+    out_so = os.path.join(BUILD, "libcaller_RWMalloc.so")
+    libdir = os.path.join(PKG, "lib")
+    cmd = ["nvcc", "-shared", "-Xcompiler", "-fPIC", "-O2", "-std=c++17",
+           "-gencode", "arch=compute_103a,code=sm_103a", '-DPBM_FAMILY_HEADER="pbm/RWMalloc.cuh"',
+           "-DPBM_WITH_MALLOC", "-I", os.path.join(ROOT, "include"),
+           os.path.join(ROOT, "tests", "caller", "dropin_caller.cu"), "-o", out_so,
+           "-L", libdir, "-lpbm", "-Xlinker", "-rpath", "-Xlinker", libdir]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    assert r.returncode == 0, r.stdout + r.stderr
+    lib = ctypes.CDLL(out_so)
+    n = 3000
+    sizes = np.clip(np.exp(np.random.default_rng(4).uniform(np.log(16), np.log(65536), n)), 16, 65536)
+    sizes = (sizes.astype(np.int32) // 4) * 4
+    out = (ctypes.c_longlong * 4)()
+    rc = lib.dropin_malloc_run(1, 4096, n, sizes.ctypes.data_as(ctypes.c_void_p), out)
+    assert rc == 0
+    bad, f0, f1, f2 = list(out)
+    assert bad == 0
+    assert f0 == 1_000_000 and f1 < f0
+    assert f2 == f0
+
+
+@pytest.fixture(scope="module")
+def pp_caller(pbm_mod):
+    os.makedirs(BUILD, exist_ok=True)
+    out_so = os.path.join(BUILD, "libcaller_parallelPage.so")
+    libdir = os.path.join(PKG, "lib")
+    cmd = ["nvcc", "-shared", "-Xcompiler", "-fPIC", "-O2", "-std=c++17",
+           "-gencode", "arch=compute_103a,code=sm_103a", "-I", os.path.join(ROOT, "include"),
+           os.path.join(ROOT, "tests", "caller", "pp_caller.cu"), "-o", out_so,
+           "-L", libdir, "-lpbm", "-Xlinker", "-rpath", "-Xlinker", libdir]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    assert r.returncode == 0, r.stdout + r.stderr
+    return ctypes.CDLL(out_so)
+
+
+@pytest.mark.parametrize("which", list(range(12)))
+def test_parallel_page_dropin(cuda, pp_caller, which):
+    """Every strategy of the monolithic API, called from a caller's kernel:
+    unique in-range pages (runs of X pages for getXPage*), payloads intact,
+    frees give the pages back."""
+    import numpy as np
+
+    n = 20000
+    ids = np.zeros(n, dtype=np.int32)
+    out = (ctypes.c_longlong * 4)()
+    rc = pp_caller.pp_run(which, n, ids.ctypes.data_as(ctypes.c_void_p), out)
+    assert rc == 0
+    bad, f0, f1, f2 = list(out)
+    assert bad == 0
+    x = {9: 4, 10: 3, 11: 2}.get(which, 1)
+    assert (ids >= 0).all() and (ids + x <= 1000000).all()
+    cover = np.zeros(1000000, dtype=np.int32)
+    for k in range(x):
+        np.add.at(cover, ids + k, 1)
+    assert cover.max() == 1
+    assert f0 - f1 == n * x
+    if which <= 8:
+        assert f2 == f0
+
+
+@pytest.mark.parametrize("which", [0, 1])
+def test_malloc_classes_dropin(cuda, pbm_mod, which):
+    """KernelMallocSimple / KernelMallocCollab passed by value into a caller's
+    kernels (unitTestMalloc1.cu shape): blocks hold their owner's bytes and
+    free() gives every page back."""
+    os.makedirs(BUILD, exist_ok=True)
+    out_so = os.path.join(BUILD, "libcaller_malloc.so")
+    if not os.path.exists(out_so):
+        libdir = os.path.join(PKG, "lib")
+        cmd = ["nvcc", "-shared", "-Xcompiler", "-fPIC", "-O2", "-std=c++17",
+               "-gencode", "arch=compute_103a,code=sm_103a", "-I", os.path.join(ROOT, "include"),
+               os.path.join(ROOT, "tests", "caller", "malloc_caller.cu"), "-o", out_so,
+               "-L", libdir, "-lpbm", "-Xlinker", "-rpath", "-Xlinker", libdir]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        assert r.returncode == 0, r.stdout + r.stderr
+    lib = ctypes.CDLL(out_so)
+    out = (ctypes.c_longlong * 4)()
+    assert lib.malloc_run(which, 20000, out) == 0
+    bad, f0, f1, f2 = list(out)
+    assert bad == 0 and f1 < f0 and f2 == f0

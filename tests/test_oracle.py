@@ -108,3 +108,28 @@ def test_cpu_churn_keeps_occupancy(orc):
     assert ok == 50000 and fail == 0
     assert orc.used_pages(w, T) == used0
     assert np.unique(held).size == held.size
+
+
+def test_malloc_replay_blocks_and_release(orc):
+    """The malloc replay packs sub-page blocks aligned to their class, gives
+    larger blocks their own runs, and the last free of a run releases it."""
+    T = 1 << 12
+    w = orc.bernoulli_bitmap(T, 0.2, 3)
+    before = w.copy()
+    rep = orc.MallocReplay(w, T, 12)
+    rng = np.random.default_rng(2)
+    sizes = np.clip(np.exp(rng.uniform(np.log(16), np.log(65536), 96)), 16, 65536).astype(np.uint64)
+    offs = []
+    for q0 in range(0, 96, 32):
+        o, _ = rep.group(sizes[q0:q0 + 32], orc.seed(9, q0), [orc.seed(10, q0 + l) for l in range(32)])
+        offs.append(o)
+    offs = np.concatenate(offs)
+    assert (offs >= 0).all()
+    cb = np.maximum(16, 1 << np.ceil(np.log2(sizes.astype(np.float64))).astype(np.int64))
+    assert (offs % np.minimum(cb, 4096) == 0).all()     # class-aligned below a page, page-aligned above
+    order = np.argsort(offs)
+    assert (offs[order][1:] >= (offs + cb)[order][:-1]).all()
+    for o in offs:
+        assert rep.free(o) == 1
+    assert rep.free(offs[0]) == 0          # double free is rejected
+    assert np.array_equal(w, before)

@@ -19,8 +19,11 @@ The L2 is flushed (512 MiB write) between timed steps, outside the events.
 
 `--impl reference` times the reference's algorithm on the host cores: the
 std::atomic replay of its word-probe walk (RandomWalkBasic_BM) over the same
-churn, all hardware threads (the reference ships no CPU implementation and its
-CUDA path is timed separately).
+churn, all hardware threads (the reference ships no CPU implementation).  The
+same line carries `reference_cuda_build`: the reference's own getPage/freePage
+(CollabRW_BM and RandomWalkBasic), compiled from its sources for sm_103a, on
+the same churn, one launch per <= 2^19 requests (its callers launch one
+thread per request; it has no batched form).
 """
 from __future__ import annotations
 
@@ -165,6 +168,7 @@ def run_reference(args, rank):
     value = tot_ops / tot_s
     sample = (f"{pairs} alloc+free pairs per step on the 2^24-page pool at 90% occupancy "
               f"(word-probe walk, reference LCG, std::atomic fetch_or/fetch_and)")
+    ref_gpu = reference_cuda_build(args)
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * tot_s / args.steps,
@@ -172,9 +176,40 @@ def run_reference(args, rank):
         "data": "synthetic", "config": workload_config(),
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "reference_cuda_build": ref_gpu,
     }
     print(json.dumps(line), flush=True)
     return 0
+
+
+def reference_cuda_build(args):
+    """The reference's own device code on the same churn (fresh pool, same
+    step request counts, L2 flushed between steps), when its cubins were built
+    (they need the reference sources at build time) and a GPU is present."""
+    try:
+        import ref_timing
+    except Exception as e:  # noqa: BLE001
+        return {"unavailable": f"reference harness not importable: {e}"}
+    if not ref_timing.available("collab"):
+        return {"unavailable": "reference cubins not built (oracle/Makefile `ref` needs the reference sources)"}
+    import oracle
+
+    n = min(args.steps, 100) + args.warmup
+    counts = group_counts(n).sum(axis=1)
+    out = {"launch": "one launch per <= 2^19 requests, 256 threads per block", "steps": n - args.warmup,
+           "warmup": args.warmup, "l2": "flushed between timed steps (512 MiB write)"}
+    for walk in ("collab", "rwbasic"):
+        words = oracle.bernoulli_bitmap(T_PAGES, OCCUPANCY, PREFILL_SEED)
+        bits = np.unpackbits(words.view(np.uint8), bitorder="little")[:T_PAGES]
+        held = np.nonzero(bits)[0].astype(np.int32)
+        np.random.default_rng(PREFILL_SEED).shuffle(held)
+        try:
+            out[walk] = ref_timing.churn(words, T_PAGES, held, counts, args.warmup, walk=walk)
+        except Exception as e:  # noqa: BLE001
+            out[walk] = {"unavailable": str(e)[:300]}
+    out["walks"] = {"collab": "CollabRW_BM.cuh getPage/freePage (warp-collaborative, atomicExch of whole words)",
+                    "rwbasic": "RandomWalkBasic.cuh getPage/freePage (page probe on an int-per-page map)"}
+    return out
 
 
 def workload_config():
@@ -386,15 +421,326 @@ def run_ours(args, rank, world, local_rank):
         "tuned_config": cfg_dict(cfg),
         "autotune_top": [dict(cfg_dict(t.cfg), ops_per_s=t.ops_per_s) for t in tuned[:6]],
     }
-    if rank == 0:
-        print(json.dumps(line), flush=True)
     graph.close()
     g_pt.close()
     pool.close()
+    del flush
+    if rank == 0 and world == 1:
+        line["configs"] = run_configs(args, torch, pbm, stream)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
     if dist:
         dist.barrier()
         dist.destroy_process_group()
     return 0
+
+
+# ----------------------------------------------------------------------------
+# The other workloads of the path, measured in the same run (keys of "configs")
+# ----------------------------------------------------------------------------
+
+def _ev_ms(torch, stream, fn):
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    fn()
+    e1.record(stream)
+    e1.synchronize()
+    return e0.elapsed_time(e1)
+
+
+def config_claim_write_free(torch, pbm, stream, reps=200):
+    """65,536 pages x 64 B (2,048-word bitmap) at 50% occupancy (seed 1);
+    32,768 threads (seed 1 + tid) each claim a page with the page-probe walk,
+    write their tid into its 64-B payload and free it."""
+    sh = stream.cuda_stream
+    T, N = 1 << 16, 1 << 15
+    out = {}
+    pool = pbm.Pool(T, 64, materialize=True)
+    pool.prefill(0.5, 1, sh)
+    before = pool.read_bitmap(sh)
+    ids = torch.empty(N, dtype=torch.int32, device="cuda")
+    steps = torch.empty(N, dtype=torch.int32, device="cuda")
+    for _ in range(5):
+        pool.claim_write_free(N, 1, ids, steps, payload_bytes=64, stream=sh)
+    ms = [_ev_ms(torch, stream, lambda: pool.claim_write_free(N, 1, ids, steps, payload_bytes=64, stream=sh))
+          for _ in range(reps)]
+    after = pool.read_bitmap(sh)
+    st = steps.cpu().numpy()
+    idv = ids.cpu().numpy()
+    out = {"pairs_per_launch": N, "launches": reps, "ms_per_launch": float(np.median(ms)),
+           "value": 2 * N / (np.median(ms) * 1e-3), "unit": "ops/s",
+           "mean_steps": float(st[idv >= 0].mean()), "failures": int((idv < 0).sum()),
+           "bitmap_restored": bool(np.array_equal(before, after)),
+           "note": "L2-resident (8 KiB bitmap, 4 MiB pages); median launch time over the launches"}
+    pool.close()
+    return out
+
+
+def config_occupancy_sweep(torch, pbm, stream, flush, rounds=16, N=1 << 22, max_steps=1024):
+    """2^24 x 4 KiB pages; occupancy {0,50,75,90,95}% (seed 2); per round one
+    launch of 2^22 get-page requests, then one freeing a uniformly random 50%
+    of that round's pages; 16 rounds.  Failures are bounded by max_steps."""
+    sh = stream.cuda_stream
+    pool = pbm.Pool(T_PAGES, PAGE_SIZE, materialize=True)
+    ids = torch.empty(N, dtype=torch.int32, device="cuda")
+    steps = torch.empty(N, dtype=torch.int32, device="cuda")
+    walks = {
+        "collab32": pbm.walk_config(pbm.COLLAB_RW_BM, word_bits=32, collab_width=32, max_steps=max_steps),
+        "word_probe32": pbm.walk_config(pbm.RANDOM_WALK_BM, word_bits=32, max_steps=max_steps),
+        "page_probe": pbm.walk_config(pbm.RANDOM_WALK, max_steps=max_steps),
+    }
+    gen = torch.Generator(device="cuda")
+    res = {}
+    for occ in (0.0, 0.5, 0.75, 0.9, 0.95):
+        row = {}
+        for wname, cfg in walks.items():
+            pool.reset(sh)
+            if occ > 0:
+                pool.prefill(occ, PREFILL_SEED, sh)
+            gen.manual_seed(PREFILL_SEED)
+            t_ms, ops, fails, round0_steps, per_round = 0.0, 0, 0, None, []
+            for r in range(rounds):
+                flush.zero_()
+                ta = _ev_ms(torch, stream, lambda: pool.alloc(cfg, N, SEED0 + 31 * r, ids, steps, stream=sh))
+                ok = ids >= 0
+                got = ids[ok]
+                if r == 0:
+                    round0_steps = float(steps[ok].double().mean().item()) if got.numel() else None
+                fails += N - int(got.numel())
+                sel = got[torch.randperm(got.numel(), generator=gen, device="cuda")[:got.numel() // 2]].contiguous()
+                flush.zero_()
+                tf = _ev_ms(torch, stream, lambda: pool.free(cfg, sel.numel(), sel, stream=sh))
+                t_ms += ta + tf
+                ops += N + sel.numel()
+                per_round.append([round(ta, 4), round(tf, 4), int(got.numel())])
+            row[wname] = {"value": ops / (t_ms * 1e-3), "ms_total": t_ms, "failures": fails,
+                          "round0_ops_s": (N + per_round[0][2] // 2) / ((per_round[0][0] + per_round[0][1]) * 1e-3),
+                          "round0_granted": per_round[0][2], "mean_steps_round0": round0_steps,
+                          "used_after": pool.used(sh), "per_round_ms_alloc_free_granted": per_round}
+        res[f"{int(occ * 100)}%"] = row
+    # the autotuner's pick per occupancy band (alloc+free swaps on held pages),
+    # then that pick against the per-thread walks on the same swaps: batched
+    # graph form, 20 steps of 256 LogU groups, L2 flushed before each step
+    tuned, churn = {}, {}
+    for occ in (0.5, 0.75, 0.9, 0.95):
+        pool.reset(sh)
+        pool.prefill(occ, PREFILL_SEED, sh)
+        words = pool.read_bitmap(sh)
+        bits = np.unpackbits(words.view(np.uint8), bitorder="little")[:T_PAGES]
+        held = np.nonzero(bits)[0].astype(np.int32)
+        np.random.default_rng(PREFILL_SEED).shuffle(held)
+        arena = torch.from_numpy(held).cuda()
+        counts = group_counts(1)
+        tab = build_descriptors(counts, len(held), pbm.OP_SWAP)
+        d_tab = torch.from_numpy(tab.view(np.uint8).reshape(-1).copy()).cuda()
+        top = pool.autotune(d_tab, N_GROUPS, int(counts[0].sum()), arena, len(held), seed=5, reps=2, stream=sh)
+        tuned[f"{int(occ * 100)}%"] = [{"walk": pbm.STRATEGY_NAMES[t.cfg.strategy], "word_bits": t.cfg.word_bits,
+                                        "width": t.cfg.collab_width, "stride": t.cfg.stride,
+                                        "blocks_per_sm": t.cfg.blocks_per_sm, "free_merge": t.cfg.free_merge,
+                                        "ops_per_s": t.ops_per_s} for t in top[:3]]
+        n_steps = 20
+        counts = group_counts(n_steps, seed=GROUP_SEED + 1)
+        tab = build_descriptors(counts, len(held), pbm.OP_SWAP)
+        d_tab = torch.from_numpy(tab.view(np.uint8).reshape(-1).copy()).cuda()
+        row = {}
+        cands = [("tuned", pbm.WalkConfig.from_buffer_copy(top[0].cfg) if top else pbm.walk_config()),
+                 ("word_probe32", pbm.walk_config(pbm.RANDOM_WALK_BM, word_bits=32)),
+                 ("page_probe", pbm.walk_config(pbm.RANDOM_WALK))]
+        for cname, cfg in cands:
+            g = pool.graph(cfg, d_tab, N_GROUPS, n_steps, arena, len(held), 4242, sh)
+            t_ms = 0.0
+            for _ in range(n_steps):
+                flush.zero_()
+                t_ms += _ev_ms(torch, stream, lambda: g.replay(sh))
+            g.close()
+            row[cname] = 2 * int(counts.sum()) / (t_ms * 1e-3)
+        chk = pool.check(arena, len(held), sh)
+        row["invariants_ok"] = bool(chk.n_duplicates == 0 and chk.n_not_marked == 0 and chk.used_pages == len(held))
+        churn[f"{int(occ * 100)}%"] = row
+    pool.close()
+    return {"rounds": rounds, "requests_per_launch": N, "max_steps": max_steps, "unit": "ops/s",
+            "ops": "get-page requests issued + pages freed", "l2": "flushed before every launch",
+            "by_occupancy": res, "autotune_by_band": tuned,
+            "churn_by_occupancy_ops_s": churn,
+            "churn_note": "alloc+free swaps on the held pages (occupancy constant), batched graph form"}
+
+
+def config_buffer_manager(torch, pbm, stream, flush, n_fetch=1 << 26, round_size=1 << 18):
+    """2^22 frames x 4 KiB over 2^24 logical pages; 2^26 fetches Zipf(0.99)
+    over a seed-3 permutation; each pin held Geometric(0.25) rounds."""
+    import workloads
+
+    sh = stream.cuda_stream
+    n_logical, n_frames = 1 << 24, 1 << 22
+    rounds = n_fetch // round_size
+    t0 = time.perf_counter()
+    pages = workloads.zipf_pages(n_logical, 0.99, n_fetch, 3)
+    ptr, idx = workloads.release_lists(rounds, round_size, 0.25, 3)
+    gen_s = time.perf_counter() - t0
+    d_pages = torch.from_numpy(pages).cuda()
+    d_idx = torch.from_numpy(idx).cuda()
+    d_frames = torch.empty(n_fetch, dtype=torch.int32, device="cuda")
+    out = {"fetches": n_fetch, "round_size": round_size, "trace_gen_s": gen_s, "unit": "fetches/s",
+           "l2": "flushed before every round"}
+    runs = [("single_clock", pbm.BM_SINGLE_CLOCK, 1, 0), ("dist_clock", pbm.BM_DIST_CLOCK, 4096, 0),
+            ("single_clock_copy4k", pbm.BM_SINGLE_CLOCK, 1, 4096)]
+    backing = None
+    for name, policy, arms, fsz in runs:
+        if fsz and backing is None:
+            backing = torch.empty(n_logical * fsz // 4, dtype=torch.int32, device="cuda")
+        bm = pbm.BufferManager(n_logical, n_frames, frame_size=fsz, policy=policy, n_arms=arms,
+                               backing=backing if fsz else None)
+        d_frames.fill_(-1)
+        t_ms = 0.0
+        for r in range(rounds):
+            a, b = int(ptr[r]), int(ptr[r + 1])
+            flush.zero_()
+            t_ms += _ev_ms(torch, stream, lambda: bm.round(d_frames, d_idx[a:] if b > a else None, b - a,
+                                                           d_pages[r * round_size:], round_size, r * round_size,
+                                                           d_frames[r * round_size:], stream=sh))
+        c = bm.counters(sh)
+        chk = bm.check(sh)
+        out[name] = {"value": n_fetch / (t_ms * 1e-3), "ms_total": t_ms, "hits": c.hits, "misses": c.misses,
+                     "evictions": c.evictions, "failures": c.failures, "hit_rate": c.hits / max(1, n_fetch),
+                     "table_mismatches": chk.mismatches, "half_loaded": chk.loading,
+                     "frame_bytes": fsz, "arms": arms}
+        bm.close()
+    del backing
+    return out
+
+
+def config_malloc(torch, pbm, stream, flush, rounds=16, plain_rounds=4):
+    """32 GiB pool of 4 KiB pages; per round 256 malloc groups (LogU[1,65536]
+    requests, sizes LogU[16 B, 64 KiB] in power-of-two classes, seed 4) and
+    frees of a uniformly random 50% of the live blocks, in one launch."""
+    sh = stream.cuda_stream
+    T = 1 << 23
+    rng = np.random.default_rng(4)
+    counts = group_counts(rounds, seed=4)
+    n_max = int(counts.sum(axis=1).max())
+    live_cap = 3 * n_max
+    gen = torch.Generator(device="cuda")
+    out = {"pool_pages": T, "page_size": PAGE_SIZE, "rounds": rounds, "unit": "ops/s",
+           "ops": "mallocs + frees", "l2": "flushed before every round"}
+    for form in ("graph", "plain"):
+        pool = pbm.Pool(T, PAGE_SIZE, materialize=True)
+        pool.malloc_init()
+        gen.manual_seed(4)
+        slots = n_max + live_cap
+        ptrs = torch.zeros(slots, dtype=torch.int64, device="cuda")
+        sizes = torch.zeros(slots, dtype=torch.int32, device="cuda")
+        n_groups = 2 * N_GROUPS
+        dt = np.dtype([("op", "<i4"), ("count", "<u4"), ("offset", "<u8")])
+        d_tab = torch.zeros(n_groups * 16, dtype=torch.uint8, device="cuda")
+        graph = pool.malloc_graph(d_tab, n_groups, 1, sizes, ptrs, slots, 91, stream=sh) if form == "graph" else None
+        live = torch.empty(0, dtype=torch.int64, device="cuda")
+        t_ms, ops, fails = 0.0, 0, 0
+        nr = rounds if form == "graph" else plain_rounds
+        for r in range(nr):
+            c = counts[r]
+            n_new = int(c.sum())
+            sz = np.clip(np.exp(rng.uniform(math.log(16), math.log(65536), n_new)), 16, 65536).astype(np.int32)
+            sizes[:n_new].copy_(torch.from_numpy(sz))
+            ptrs[:n_new].zero_()
+            k = live.numel() // 2
+            perm = torch.randperm(live.numel(), generator=gen, device="cuda")
+            to_free, keep = live[perm[:k]], live[perm[k:]]
+            ptrs[n_max:n_max + k].copy_(to_free)
+            tab = np.zeros(n_groups, dtype=dt)
+            offs = np.concatenate([[0], np.cumsum(c)[:-1]])
+            tab["op"][:N_GROUPS] = pbm.OP_MALLOC
+            tab["count"][:N_GROUPS] = c
+            tab["offset"][:N_GROUPS] = offs
+            fsplit = np.linspace(0, k, N_GROUPS + 1).astype(np.int64)
+            tab["op"][N_GROUPS:] = pbm.OP_MFREE
+            tab["count"][N_GROUPS:] = np.diff(fsplit)
+            tab["offset"][N_GROUPS:] = n_max + fsplit[:-1]
+            d_tab.copy_(torch.from_numpy(tab.view(np.uint8).copy()))
+            flush.zero_()
+            if graph is not None:
+                t_ms += _ev_ms(torch, stream, lambda: graph.replay(sh))
+            else:
+                hg = pbm.groups_array([(int(t["op"]), int(t["count"]), int(t["offset"])) for t in tab])
+                t_ms += _ev_ms(torch, stream, lambda: pool.malloc_batch(d_tab, hg, n_groups, sizes, ptrs, slots,
+                                                                        1000 + r, pbm.LAUNCH_PLAIN, stream=sh))
+            new = ptrs[:n_new]
+            ok = new != 0
+            fails += n_new - int(ok.sum().item())
+            live = torch.cat([keep, new[ok]])
+            if live.numel() > live_cap:
+                live = live[:live_cap]
+            ops += n_new + k
+        lv, bad = pool.malloc_counts(sh)
+        out[form] = {"value": ops / (t_ms * 1e-3), "ms_total": t_ms, "rounds": nr, "failures": fails,
+                     "live_blocks": int(lv), "bad_frees": int(bad), "used_pages": pool.used(sh)}
+        if graph is not None:
+            graph.close()
+        pool.close()
+    out["graph_over_plain"] = out["graph"]["value"] / out["plain"]["value"]
+    return out
+
+
+def config_serving(torch, pbm, stream, rates=(1e5, 1e6, 1e7, 1e8, 1e9), min_req=100, max_req=20000,
+                   horizon_s=1.0):
+    """64 tenants, Poisson arrivals at an aggregate page rate, batches
+    LogU[1,65536] pages, mix 45% alloc / 45% free / 10% Zipf(0.99) fetch,
+    seed 5; 2^24-page pool prefilled to 80%, budget 95%."""
+    import workloads
+
+    T = T_PAGES
+    tenants = 64
+    fetch = torch.from_numpy(workloads.zipf_pages(T, 0.99, 1 << 24, 5)).cuda()
+    mean_pages = (MAX_GROUP - 1) / math.log(MAX_GROUP)
+    out = {"tenants": tenants, "pool_pages": T, "prefill": 0.8, "max_occupancy": 0.95,
+           "unit": "pages/s", "rates": {}}
+    for rate in rates:
+        rng = np.random.default_rng(5)
+        n = int(min(max_req, max(min_req, rate * horizon_s / mean_pages)))
+        cnt = np.clip(np.floor(np.exp(rng.uniform(0, math.log(MAX_GROUP + 1), n))), 1, MAX_GROUP).astype(np.int64)
+        arr = np.cumsum(rng.exponential(mean_pages / rate, n))
+        ten = rng.integers(0, tenants, n)
+        u = rng.uniform(size=n)
+        ops = np.where(u < 0.45, 0, np.where(u < 0.90, 1, 2))
+        pool = pbm.Pool(T, PAGE_SIZE)
+        pool.prefill(0.8, PREFILL_SEED)
+        bm = pbm.BufferManager(T, 1 << 22, policy=pbm.BM_DIST_CLOCK, n_arms=4096)
+        srv = pbm.Server(pool, tenants, 1 << 16, n_streams=4, max_batch_requests=256, max_occupancy=0.95,
+                         bufmgr=bm, fetch_pages=fetch, max_fetch_pages=1 << 20)
+        res, rep, rc = srv.run(arr, ten, ops, cnt)
+        st = np.array([r.status for r in res])
+        out["rates"][f"{rate:.0e}"] = {
+            "requests": n, "arrival_span_s": float(arr[-1]), "wall_s": rep.wall_s,
+            "throughput": rep.pages / rep.wall_s, "p50_ms": rep.p50_s * 1e3, "p99_ms": rep.p99_s * 1e3,
+            "batches": rep.batches, "mean_batch_requests": rep.mean_batch_requests,
+            "max_in_flight": rep.max_in_flight, "over_budget": int((st == pbm.ERR_EXHAUSTED).sum()),
+            "rc": rc}
+        srv.close()
+        bm.close()
+        pool.close()
+    return out
+
+
+def run_configs(args, torch, pbm, stream):
+    flush = torch.empty(512 << 20, dtype=torch.uint8, device="cuda")
+    todo = [("claim_write_free_50pct", lambda: config_claim_write_free(torch, pbm, stream)),
+            ("occupancy_sweep", lambda: config_occupancy_sweep(torch, pbm, stream, flush)),
+            ("buffer_manager", lambda: config_buffer_manager(torch, pbm, stream, flush)),
+            ("malloc", lambda: config_malloc(torch, pbm, stream, flush)),
+            ("serving", lambda: config_serving(torch, pbm, stream))]
+    want = set(args.configs.split(",")) if args.configs not in ("all", "none") else None
+    out = {}
+    for name, fn in todo:
+        if args.configs == "none" or (want is not None and name not in want):
+            continue
+        t0 = time.perf_counter()
+        try:
+            out[name] = fn()
+        except Exception as e:  # noqa: BLE001 -- one workload's error must not hide the others
+            out[name] = {"error": f"{type(e).__name__}: {e}"[:400]}
+        out[name]["wall_s"] = time.perf_counter() - t0
+        torch.cuda.synchronize()
+    return out
 
 
 def run_profile_case(args):
@@ -456,6 +802,9 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--profile", action="store_true", help="batched form only (for ncu)")
     ap.add_argument("--profile-walk", default="collab32", choices=["collab32", "collab64", "word32"])
+    ap.add_argument("--configs", default="all",
+                    help="other workloads measured after the headline: all, none, or a comma list of "
+                         "claim_write_free_50pct,occupancy_sweep,buffer_manager,malloc,serving")
     args = ap.parse_args()
     rank, world, local_rank = env_rank()
     if args.profile:

@@ -196,9 +196,10 @@ int pbm_batch_launch(pbm_pool *pool, const pbm_walk_config *cfg, const pbm_group
                      const pbm_group *h_groups, uint32_t n_groups, int32_t *d_arena,
                      uint64_t arena_len, uint32_t seed, int32_t *d_steps, int mode, void *stream);
 
-/* Graph-replayed persistent batch.  The descriptors of step k are read from
- * d_groups + k*n_groups with seed seed0 + k, where k is a device-resident
- * counter that each replay advances; replay with pbm_graph_replay. */
+/* Graph-replayed persistent batch.  Replay k reads the descriptors at
+ * d_groups + (k mod n_steps)*n_groups with seed seed0 + k, where k is a
+ * device-resident counter that each replay advances (pbm_graph_set_step sets
+ * it); replay with pbm_graph_replay, any number of times. */
 typedef struct pbm_graph pbm_graph;
 int pbm_batch_graph_create(pbm_pool *pool, const pbm_walk_config *cfg, const pbm_group *d_groups,
                            uint32_t n_groups, uint32_t n_steps, int32_t *d_arena,
@@ -227,7 +228,7 @@ int pbm_malloc_tables(pbm_pool *pool, void **d_start_of, void **d_live, void **d
 int pbm_malloc_batch(pbm_pool *pool, const pbm_group *d_groups, const pbm_group *h_groups, uint32_t n_groups,
                      const uint32_t *d_sizes, unsigned long long *d_ptrs, uint64_t arena_len, uint32_t seed,
                      uint32_t max_steps, int mode, void *stream);
-/* Graph form: step k reads d_groups + k*n_groups with seed seed0 + k. */
+/* Graph form: replay k reads d_groups + (k mod n_steps)*n_groups with seed seed0 + k. */
 int pbm_malloc_graph_create(pbm_pool *pool, const pbm_group *d_groups, uint32_t n_groups, uint32_t n_steps,
                             const uint32_t *d_sizes, unsigned long long *d_ptrs, uint64_t arena_len,
                             uint32_t seed0, uint32_t max_steps, void *stream, pbm_graph **out);
@@ -310,12 +311,16 @@ int pbm_bufmgr_gather(pbm_bufmgr *m, const int32_t *d_frame_ids, uint32_t n, uin
  * ALLOC n: n new pages appended to the tenant's ring of page slots.
  * FREE n:  releases min(n, pages the tenant holds) of its oldest pages.
  * FETCH n: pins then releases the next n pages of the shared fetch trace.
- * A tenant's requests are admitted in arrival order; an ALLOC waits until
- * held pages stay <= max_occupancy of the pool, a FREE until the pages it
- * releases are allocated on the device.  Admitted requests of all tenants
- * form the next batch whenever one of n_streams batch slots is free, so
- * batches overlap on the device.  Page counts per request depend only on
- * the tenant's own requests (results do not depend on the mix). */
+ * A tenant's requests are admitted in arrival order.  Admission is by
+ * free-page budget: each tenant may hold at most tenant_quota_pages (0 = the
+ * pages free below max_occupancy at create time, split evenly), and an ALLOC
+ * that would exceed it is rejected (status PBM_ERR_EXHAUSTED) -- only the
+ * tenant's own later FREEs could make room, and they queue behind it.  A
+ * FREE waits until the pages it releases are allocated on the device.
+ * Admitted requests of all tenants form the next batch whenever one of
+ * n_streams batch slots is free, so batches overlap on the device.  Page
+ * counts and statuses per request depend only on the tenant's own requests
+ * and quota (results do not depend on the mix). */
 #define PBM_REQ_ALLOC 0
 #define PBM_REQ_FREE  1
 #define PBM_REQ_FETCH 2
@@ -331,7 +336,7 @@ typedef struct {
 typedef struct {
     double   admit_s, launch_s, done_s, latency_s;   /* seconds since the run started */
     uint64_t pages;        /* pages allocated / released / fetched */
-    int32_t  status;       /* 0 done, -1 never admitted */
+    int32_t  status;       /* 0 done, PBM_ERR_EXHAUSTED over budget, -1 never admitted */
     uint32_t reserved;
 } pbm_request_result;
 
@@ -341,8 +346,8 @@ typedef struct {
     uint32_t n_streams;           /* batches in flight at most */
     uint32_t max_batch_requests;  /* requests per batch at most (<= 2048) */
     uint32_t max_fetch_pages;     /* fetch pages per batch at most (0 = 1<<22) */
-    uint32_t reserved;
-    double   max_occupancy;       /* admission bound on held pages / pool pages */
+    uint32_t tenant_quota_pages;  /* pages a tenant may hold (0 = even split, see above) */
+    double   max_occupancy;       /* bound on held pages / pool pages (sets the default quota) */
     double   drain_timeout_s;     /* stop waiting this long after the last arrival */
     pbm_walk_config walk;         /* allocation walk of the batches */
 } pbm_server_config;

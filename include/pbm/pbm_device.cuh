@@ -217,24 +217,46 @@ __device__ __forceinline__ int32_t walk_word(const PoolView& v, int32_t seed0,
 // ---------------------------------------------------------------------------
 // Warp-collaborative walk (CollabRW_BM, source/CollabRW_BM.cuh:114-160,
 // restated lock-free).  A group of W lanes (W = 8, 16 or 32, aligned within
-// the warp) shares one LCG stream.  Per iteration lane i reads word
+// the warp) shares one LCG stream.  Per jump lane i reads word
 // (base + i*stride) mod L with one coalesced load when stride == 1; the
 // group claims exactly as many clear bits as it still needs -- lowest lanes
 // and lowest bits first, one atomicOr per word -- and hands the bits it
-// gained to the needing lanes in lane order.  Nothing is over-claimed, so
-// nothing is written back.  Lanes whose words coincide (only possible when
-// W*stride > L) are de-duplicated with __match_any_sync.
+// gained to the needing lanes in lane order (needing lane of rank r takes
+// the r-th gained bit).  Nothing is over-claimed, so nothing is written back.
+// When a concurrent claim took some of the planned bits, the group plans
+// once more in the same words from the values its atomics returned (no new
+// load, no new jump) before it jumps again.  Lanes whose words coincide
+// (only possible when W*stride > L) are de-duplicated with __match_any_sync.
 //
 // Every lane of the group must call this converged; `need` says whether the
 // lane requests a page.  All lanes of the group report the same step count
-// (iterations of the group), as in the reference.  `slots` is a per-group
-// scratch of W ints in shared memory.
+// (jumps of the group), as in the reference.  `slots` is unused (kept for
+// the callers' shared scratch layout).
 // ---------------------------------------------------------------------------
+template <int W>
+__device__ __forceinline__ int group_incl_scan(int v, uint32_t gl, uint32_t gmask) {
+#pragma unroll
+    for (int d = 1; d < W; d <<= 1) {
+        int y = __shfl_up_sync(gmask, v, d, W);
+        if ((int)gl >= d) v += y;
+    }
+    return v;
+}
+
+// Position of the (k+1)-th set bit of m (k < popc(m)).
+__device__ __forceinline__ uint32_t nth_bit(uint32_t m, int k) { return __fns(m, 0u, k + 1); }
+__device__ __forceinline__ uint32_t nth_bit(uint64_t m, int k) {
+    const uint32_t lo = (uint32_t)m;
+    const int c = __popc(lo);
+    return k < c ? __fns(lo, 0u, k + 1) : 32u + __fns((uint32_t)(m >> 32), 0u, k - c + 1);
+}
+
 template <int W, typename Word>
 __device__ __forceinline__ int32_t walk_collab(const PoolView& v, bool need, int32_t group_seed,
                                                uint32_t lane_off /* (lane_in_group*stride) % L */,
                                                bool dedupe, uint32_t max_steps,
                                                volatile int32_t* slots, int32_t* steps_out) {
+    (void)slots;
     using T = WordTraits<Word>;
     Word* words = reinterpret_cast<Word*>(v.words);
     const uint32_t L = T::count(v);
@@ -251,57 +273,61 @@ __device__ __forceinline__ int32_t walk_collab(const PoolView& v, bool need, int
         x = lcg31(x);
         uint32_t w = idx_hi(x, L) + lane_off;
         if (w >= L) w -= L;
-        Word val = load_word(words + w);
+        Word fr = (Word)~load_word(words + w);
         if (dedupe) {
             uint32_t peers = __match_any_sync(gmask, w);
-            if ((peers & lt) != 0u) val = T::full();               // a lower lane reads this word
+            if ((peers & lt) != 0u) fr = 0;                          // a lower lane reads this word
         }
-        Word fr = (Word)~val;
-        int cnt = popc_w(fr);
-        // inclusive scan of cnt over the group
-        int incl = cnt;
-#pragma unroll
-        for (int d = 1; d < W; d <<= 1) {
-            int y = __shfl_up_sync(gmask, incl, d, W);
-            if ((int)gl >= d) incl += y;
-        }
-        int n = __popc(needm);
-        int pre = incl - cnt;
-        Word m = low_bits(fr, n - pre);
-        Word got = 0;
-        if (m) {
-            Word old = atomic_or(words + w, m);
-            got = m & (Word)~old;
-        }
-        int g = popc_w(got);
-        int gincl, G;
-        if (__ballot_sync(gmask, got != m) == 0u) {
-            // every planned bit stuck: lane i gained exactly its share, so the
-            // prefix of gains is the capped prefix of free bits
-            gincl = min(incl, n);
-            G = min(__shfl_sync(gmask, incl, W - 1, W), n);
-        } else {
-            gincl = g;
-#pragma unroll
-            for (int d = 1; d < W; d <<= 1) {
-                int y = __shfl_up_sync(gmask, gincl, d, W);
-                if ((int)gl >= d) gincl += y;
+        for (int pass = 0;; ++pass) {
+            const int cnt = popc_w(fr);
+            const int incl = group_incl_scan<W>(cnt, gl, gmask);
+            const int n = __popc(needm);
+            const Word m = low_bits(fr, n - (incl - cnt));
+            Word got = 0, old = 0;
+            if (m) {
+                old = atomic_or(words + w, m);
+                got = m & (Word)~old;
             }
-            G = __shfl_sync(gmask, gincl, W - 1, W);
+            const bool lost = __ballot_sync(gmask, got != m) != 0u;
+            const int g = popc_w(got);
+            // inclusive prefix of the bits gained, and their total
+            int gincl, G;
+            if (!lost) {
+                // every planned bit stuck: the gains are the capped free-bit prefix
+                gincl = min(incl, n);
+                G = min(__shfl_sync(gmask, incl, W - 1, W), n);
+            } else {
+                gincl = group_incl_scan<W>(g, gl, gmask);
+                G = __shfl_sync(gmask, gincl, W - 1, W);
+            }
+            if (G > 0) {
+                // needing lane of rank r takes gained bit r: its source is the
+                // first group lane whose inclusive gain exceeds r
+                const int r = need && id < 0 ? __popc(needm & lt) : 0;
+                int src = 0;
+#pragma unroll
+                for (int step = W / 2; step >= 1; step >>= 1) {
+                    const int gv = __shfl_sync(gmask, gincl, src + step - 1, W);
+                    if (gv <= r) src += step;
+                }
+                const int src_excl = __shfl_sync(gmask, gincl - g, src, W);
+                const uint32_t src_w = __shfl_sync(gmask, w, src, W);
+                Word src_got;
+                if constexpr (sizeof(Word) == 8) {
+                    const uint32_t lo = __shfl_sync(gmask, (uint32_t)got, src, W);
+                    const uint32_t hi = __shfl_sync(gmask, (uint32_t)(got >> 32), src, W);
+                    src_got = ((Word)hi << 32) | (Word)lo;
+                } else {
+                    src_got = __shfl_sync(gmask, got, src, W);
+                }
+                if (need && id < 0 && r < G)
+                    id = (int32_t)((src_w << T::kShift) + nth_bit(src_got, r - src_excl));
+            }
+            needm = __ballot_sync(gmask, need && id < 0);
+            if (!needm || !lost || pass > 0) break;
+            // plan again in the same words: the atomics returned their state
+            if (m) fr = (Word)~(old | m);
         }
-        int pos = gincl - g;
-        while (got) {
-            int b = ctz_w(got);
-            got &= got - (Word)1;
-            slots[pos++] = (int32_t)(((uint32_t)w << T::kShift) + (uint32_t)b);
-        }
-        __syncwarp(gmask);
-        if (id < 0 && need) {
-            int rank = __popc(needm & lt);
-            if (rank < G) id = slots[rank];
-        }
-        __syncwarp(gmask);
-        needm = __ballot_sync(gmask, need && id < 0);
     }
     if (steps_out) *steps_out = (int32_t)s;
     return id;

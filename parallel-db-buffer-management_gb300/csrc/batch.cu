@@ -21,7 +21,8 @@ struct BatchArgs {
     PoolView v;
     const pbm_group* groups;            // base of the descriptor table
     uint32_t n_groups;
-    uint32_t* d_step;                   // graph form: step counter (may be null)
+    uint32_t* d_step;                   // graph form: replay counter (may be null)
+    uint32_t n_steps;                   // graph form: descriptor tables (replay k uses k mod n_steps)
     uint32_t seed;
     int32_t* arena;
     unsigned long long arena_len;
@@ -78,6 +79,8 @@ __device__ __forceinline__ void batch_round(const BatchArgs& a, uint32_t seed, b
                                             unsigned long long q, unsigned long long slot,
                                             uint32_t lane_off, volatile int32_t* gslots, BAcc& acc) {
     const bool need = active && (op == PBM_OP_ALLOC || op == PBM_OP_SWAP);
+    // the slot's held page is read before the walk so its latency overlaps it
+    const int32_t held = (active && op != PBM_OP_ALLOC) ? a.arena[slot] : -1;
     int32_t s = 0, id = -1;
     if constexpr (K == BWalk::Collab) {
         const uint32_t gl = threadIdx.x & (uint32_t)(W - 1);
@@ -93,14 +96,11 @@ __device__ __forceinline__ void batch_round(const BatchArgs& a, uint32_t seed, b
     if (active) {
         if (op == PBM_OP_ALLOC) {
             a.arena[slot] = id;
-        } else {
-            int32_t old = a.arena[slot];
-            if (op == PBM_OP_FREE) {
-                to_free = old;
-            } else if (id >= 0) {           // swap
-                a.arena[slot] = id;
-                to_free = old;
-            }
+        } else if (op == PBM_OP_FREE) {
+            to_free = held;
+        } else if (id >= 0) {               // swap
+            a.arena[slot] = id;
+            to_free = held;
         }
         if (to_free >= (int32_t)a.v.n_pages) to_free = -1;
         if (need) {
@@ -137,7 +137,7 @@ __global__ void __launch_bounds__(256, MINB) k_batch_persistent(BatchArgs a) {
     __shared__ bool s_last;
     BAcc acc;
     const uint32_t step = a.d_step ? *a.d_step : 0u;
-    const pbm_group* groups = a.groups + (size_t)step * a.n_groups;
+    const pbm_group* groups = a.groups + (a.d_step ? (size_t)(step % a.n_steps) * a.n_groups : 0);
     const uint32_t seed = a.seed + step;
     const unsigned long long* pre = a.prefix;
     if (a.fuse) {
@@ -152,6 +152,7 @@ __global__ void __launch_bounds__(256, MINB) k_batch_persistent(BatchArgs a) {
     volatile int32_t* gslots = slots + (threadIdx.x & ~(uint32_t)(W - 1));
     const unsigned long long warp0 = ((unsigned long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const unsigned long long nwarps = ((unsigned long long)gridDim.x * blockDim.x) >> 5;
+    uint32_t g_next = 0xffffffffu;     // lane 0: group of the next chunk, found while prefetching
     for (unsigned long long chunk = warp0; chunk * 32ull < total; chunk += nwarps) {
         const unsigned long long q0 = chunk * 32ull;
         const unsigned long long q = q0 + lane;
@@ -159,10 +160,11 @@ __global__ void __launch_bounds__(256, MINB) k_batch_persistent(BatchArgs a) {
         // group of the chunk's first request: one lane searches, the warp shares
         uint32_t g0 = 0;
         if (lane == 0) {
-            g0 = find_group_any(pre, a.n_groups, q0, 0u);
+            g0 = g_next != 0xffffffffu ? g_next : find_group_any(pre, a.n_groups, q0, 0u);
             const unsigned long long nq0 = q0 + nwarps * 32ull;
             if (nq0 < total) {
                 const uint32_t ng = find_group_any(pre, a.n_groups, nq0, g0);
+                g_next = ng;
                 const unsigned long long ns = wrap_slot(groups[ng].offset + (nq0 - pre[ng]), a.arena_len);
                 prefetch_l2(a.arena + ns);
                 prefetch_l2(a.arena + wrap_slot(ns + 31ull, a.arena_len));
@@ -399,7 +401,7 @@ int pbm_batch_launch(pbm_pool* pool, const pbm_walk_config* cfg, const pbm_group
         }
         pool->prefix_cap = n_groups + 1u;
     }
-    k_batch_prefix<<<1, 1024, 0, s>>>(d_groups, n_groups, nullptr, pool->d_prefix);
+    k_batch_prefix<<<1, 1024, 0, s>>>(d_groups, n_groups, nullptr, 1u, pool->d_prefix);
     PBM_LAUNCH_CHECK();
     a.groups = d_groups;
     a.n_groups = n_groups;
@@ -439,6 +441,7 @@ int pbm_batch_graph_create(pbm_pool* pool, const pbm_walk_config* cfg, const pbm
     a.n_groups = n_groups;
     a.prefix = g->d_prefix;
     a.d_step = g->d_step;
+    a.n_steps = n_steps;
     a.done = g->d_done;                       // the last block advances the step
     a.fuse = n_groups <= kFusedGroups ? 1 : 0;
     // Capture on a private stream (the legacy default stream cannot be
@@ -459,7 +462,7 @@ int pbm_batch_graph_create(pbm_pool* pool, const pbm_walk_config* cfg, const pbm
         return PBM_ERR_CUDA;
     }
     if (!a.fuse) {
-        k_batch_prefix<<<1, 1024, 0, cap>>>(d_groups, n_groups, g->d_step, g->d_prefix);
+        k_batch_prefix<<<1, 1024, 0, cap>>>(d_groups, n_groups, g->d_step, n_steps, g->d_prefix);
         count_launch();
     }
     rc = launch_batch(&c2, a, true, cap);

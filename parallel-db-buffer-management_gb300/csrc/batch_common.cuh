@@ -73,9 +73,11 @@ __device__ __forceinline__ void block_exclusive_prefix(const pbm_group* g, uint3
 }
 
 // Exclusive prefix of one step's groups (one block of 1024 threads).
+// Graph forms keep a monotone replay counter; replay k reads descriptor table
+// k mod n_steps (so a graph may be replayed any number of times).
 __global__ void k_batch_prefix(const pbm_group* groups, uint32_t n_groups, const uint32_t* d_step,
-                               unsigned long long* prefix) {
-    const uint32_t step = d_step ? *d_step : 0u;
+                               uint32_t n_steps, unsigned long long* prefix) {
+    const uint32_t step = d_step ? *d_step % n_steps : 0u;
     block_exclusive_prefix(groups + (size_t)step * n_groups, n_groups, prefix);
 }
 

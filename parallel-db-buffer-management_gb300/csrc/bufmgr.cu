@@ -7,10 +7,12 @@
 //
 //   page_table[p]   frame holding logical page p, -1 not resident, -2 being
 //                   loaded by another request
-//   frame_state[f]  (page << 32) | pins in one 64-bit word, so a fetch pins a
-//                   frame only if it still holds its page, and a sweep takes a
-//                   frame only if it is unpinned and unchanged -- each with one
-//                   compare-and-swap
+//   frame_state[f]  (page << 32) | pins in one 64-bit word.  A fetch pins with
+//                   one atomicAdd and keeps the pin only if the word it added
+//                   to still named its page (else it subtracts it again), so
+//                   hot frames see no compare-and-swap retries; a sweep takes
+//                   a frame only if it is unpinned and unchanged (one CAS), so
+//                   a pin in flight makes the sweep pass the frame by
 //   ref[f]          CLOCK reference bit, set on every fetch
 //   arms            SINGLE: one shared hand (atomicAdd); DIST: per-slot hands,
 //                   each starting at its own frame and advancing privately
@@ -21,7 +23,9 @@
 // unreferenced frame, unmap its old page (eviction), optionally copy the
 // page from the backing store, map p (miss).  A fetch that finds no frame
 // within max_sweep hand steps fails (-1) instead of spinning; waits on a
-// loading page are bounded too.
+// loading page are bounded too.  Lanes of a warp that fetch the same page
+// pin it with one atomicAdd of their count (Zipf streams repeat hot pages
+// within a warp).
 #include <cstring>
 #include <new>
 
@@ -87,19 +91,23 @@ struct BmAcc {
     unsigned long long hits = 0, misses = 0, evictions = 0, failures = 0, timeouts = 0;
 };
 
+// Adds k pins to frame f if it holds `page`; otherwise leaves it unchanged
+// (the add is taken back) and returns false.
+__device__ __forceinline__ bool pin_if_owner(const BmView& b, int32_t f, uint32_t page, uint32_t k) {
+    const unsigned long long old = atomicAdd(b.frame_state + f, (unsigned long long)k);
+    if ((uint32_t)(old >> 32) == page) return true;
+    atomicAdd(b.frame_state + f, 0ull - (unsigned long long)k);
+    return false;
+}
+
 __device__ __forceinline__ int32_t fetch(const BmView& b, uint32_t page, uint32_t slot, BmAcc& acc) {
     for (uint32_t attempt = 0; attempt < kFetchSpinLimit; ++attempt) {
         int32_t f = __ldcg(b.page_table + page);
         if (f >= 0) {
-            unsigned long long s = __ldcg(b.frame_state + f);
-            while ((uint32_t)(s >> 32) == page) {
-                unsigned long long old = atomicCAS(b.frame_state + f, s, s + 1ull);
-                if (old == s) {
-                    b.ref[f] = 1;
-                    ++acc.hits;
-                    return f;
-                }
-                s = old;
+            if (pin_if_owner(b, f, page, 1u)) {
+                b.ref[f] = 1;
+                ++acc.hits;
+                return f;
             }
             continue;   // the frame changed owner: read the page table again
         }
@@ -135,13 +143,14 @@ __device__ __forceinline__ int32_t fetch(const BmView& b, uint32_t page, uint32_
 
 __device__ __forceinline__ void unpin(const BmView& b, int32_t f, unsigned long long& ok, unsigned long long& bad) {
     if (f < 0 || (uint32_t)f >= b.n_frames) return;
-    unsigned long long s = __ldcg(b.frame_state + f);
-    for (;;) {
-        if ((uint32_t)s == 0u) { ++bad; return; }
-        unsigned long long old = atomicCAS(b.frame_state + f, s, s - 1ull);
-        if (old == s) { ++ok; return; }
-        s = old;
+    if ((uint32_t)__ldcg(b.frame_state + f) == 0u) { ++bad; return; }   // nothing pinned
+    const unsigned long long old = atomicAdd(b.frame_state + f, ~0ull);
+    if ((uint32_t)old == 0u) {          // a racing unpin of the same pin took it first
+        atomicAdd(b.frame_state + f, 1ull);
+        ++bad;
+        return;
     }
+    ++ok;
 }
 
 // One round: release the listed pins, then fetch this round's pages.
@@ -157,13 +166,44 @@ __global__ void __launch_bounds__(256) k_round(BmView b, const int32_t* release_
         int32_t idx = release_idx[j];
         unpin(b, release_frames_of[idx], ok, bad);
     }
-    if (nthr == 1u) __threadfence();
     BmAcc acc;
-    for (uint32_t i = tid; i < n; i += nthr) {
-        int32_t p = pages[i];
-        int32_t f = -1;
-        if (p >= 0 && (uint32_t)p < b.n_logical) f = fetch(b, (uint32_t)p, (slot0 + i) % b.n_arms, acc);
-        frames_out[i] = f;
+    if (nthr == 1u) {
+        __threadfence();
+        for (uint32_t i = 0; i < n; ++i) {
+            int32_t p = pages[i];
+            int32_t f = -1;
+            if (p >= 0 && (uint32_t)p < b.n_logical) f = fetch(b, (uint32_t)p, (slot0 + i) % b.n_arms, acc);
+            frames_out[i] = f;
+        }
+    } else {
+        // warp-uniform trip count (blockDim is a multiple of 32), so the warp
+        // can merge the pins of lanes fetching the same page
+        const uint32_t lane = threadIdx.x & 31u;
+        for (uint32_t base = tid - lane; base < n; base += nthr) {
+            const uint32_t i = base + lane;
+            const int32_t p = i < n ? pages[i] : -1;
+            const bool valid = p >= 0 && (uint32_t)p < b.n_logical;
+            const uint32_t key = valid ? (uint32_t)p : 0x80000000u + lane;   // invalid lanes never merge
+            const uint32_t peers = __match_any_sync(0xffffffffu, key);
+            const uint32_t leader = (uint32_t)__ffs((int)peers) - 1u;
+            int32_t hit = -1;
+            if (valid && lane == leader) {
+                const int32_t f0 = __ldcg(b.page_table + p);
+                if (f0 >= 0 && pin_if_owner(b, f0, (uint32_t)p, (uint32_t)__popc(peers))) {
+                    b.ref[f0] = 1;
+                    hit = f0;
+                }
+            }
+            hit = __shfl_sync(0xffffffffu, hit, (int)leader);
+            int32_t f = -1;
+            if (hit >= 0) {
+                f = hit;
+                ++acc.hits;
+            } else if (valid) {
+                f = fetch(b, (uint32_t)p, (slot0 + i) % b.n_arms, acc);
+            }
+            if (i < n) frames_out[i] = f;
+        }
     }
     if (ok) atomicAdd(&b.stats->unpins, ok);
     if (bad) atomicAdd(&b.stats->bad_unpins, bad);

@@ -18,6 +18,7 @@ struct MArgs {
     const pbm_group* groups;
     uint32_t n_groups;
     const uint32_t* d_step;
+    uint32_t n_steps;                 // graph form: replay k uses descriptor table k mod n_steps
     uint32_t seed;
     const uint32_t* sizes;            // per slot
     unsigned long long* ptrs;         // per slot (device addresses, 0 = none)
@@ -81,7 +82,7 @@ template <bool SERIAL>
 __global__ void __launch_bounds__(256) k_malloc_persistent(MArgs a) {
     MAcc acc;
     const uint32_t step = a.d_step ? *a.d_step : 0u;
-    const pbm_group* groups = a.groups + (size_t)step * a.n_groups;
+    const pbm_group* groups = a.groups + (a.d_step ? (size_t)(step % a.n_steps) * a.n_groups : 0);
     const uint32_t seed = a.seed + step;
     const unsigned long long total = a.prefix[a.n_groups];
     const uint32_t lane = threadIdx.x & 31u;
@@ -273,7 +274,7 @@ int pbm_malloc_batch(pbm_pool* pool, const pbm_group* d_groups, const pbm_group*
         }
         t->prefix_cap = n_groups + 1u;
     }
-    k_batch_prefix<<<1, 1024, 0, s>>>(d_groups, n_groups, nullptr, t->prefix);
+    k_batch_prefix<<<1, 1024, 0, s>>>(d_groups, n_groups, nullptr, 1u, t->prefix);
     PBM_LAUNCH_CHECK();
     a.groups = d_groups;
     a.n_groups = n_groups;
@@ -314,6 +315,7 @@ int pbm_malloc_graph_create(pbm_pool* pool, const pbm_group* d_groups, uint32_t 
     a.groups = d_groups;
     a.n_groups = n_groups;
     a.d_step = g->d_step;
+    a.n_steps = n_steps;
     a.seed = seed0;
     a.sizes = d_sizes;
     a.ptrs = d_ptrs;
@@ -328,7 +330,7 @@ int pbm_malloc_graph_create(pbm_pool* pool, const pbm_group* d_groups, uint32_t 
     PBM_CUDA_TRY(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
     cudaError_t e = cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal);
     if (e == cudaSuccess) {
-        k_batch_prefix<<<1, 1024, 0, cap>>>(d_groups, n_groups, g->d_step, g->d_prefix);
+        k_batch_prefix<<<1, 1024, 0, cap>>>(d_groups, n_groups, g->d_step, n_steps, g->d_prefix);
         k_malloc_persistent<false><<<sm_count() * per_sm, 256, 0, cap>>>(a);
         k_step_advance<<<1, 32, 0, cap>>>(g->d_step);
         cudaGraph_t graph = nullptr;

@@ -6,15 +6,18 @@
 // page slots in device memory: ALLOC n appends n new pages, FREE n releases
 // min(n, pages the tenant holds) of its oldest pages, FETCH n pins and then
 // releases n pages of a shared fetch trace in the buffer manager.  A tenant's
-// requests are admitted in arrival order; an ALLOC waits for free-page budget
-// (held pages stay at or below max_occupancy of the pool), a FREE waits until
-// the pages it releases have been allocated on the device.  Admitted requests
+// requests are admitted in arrival order.  Admission is by free-page budget:
+// the pages free below max_occupancy when the server is created are split
+// into per-tenant quotas, and an ALLOC that would take its tenant over quota
+// is rejected at once (the tenant's own later FREEs, which could make room,
+// queue behind it, so waiting could only deadlock).  A FREE waits until the
+// pages it releases have been allocated on the device.  Admitted requests
 // of all tenants form the next batch as soon as one of n_streams batch slots
 // is free, so batches overlap on the device and requests that arrive while
 // others run join the following batch.  Bitmap, clock hands, rings and RNG
 // streams stay resident between batches.  Page counts per request depend only
-// on the tenant's own requests, so a tenant gets the same results alone and
-// in a mix; only latencies change.
+// on the tenant's own requests and quota, so a tenant gets the same results
+// alone and in a mix; only latencies change.
 #include <algorithm>
 #include <chrono>
 #include <deque>
@@ -65,6 +68,7 @@ struct pbm_server {
     uint32_t max_groups;
     uint32_t max_fetch;
     uint64_t n_pages;
+    uint64_t quota;                  // pages a tenant may hold
     uint32_t seed;
     uint64_t fetch_cursor;
     std::vector<Tenant> tenants;
@@ -93,6 +97,15 @@ int pbm_server_create(pbm_pool* pool, pbm_bufmgr* bm, const int32_t* d_fetch_pag
     s->seed = 0x51u;
     s->fetch_cursor = 0;
     s->tenants.resize(cfg->n_tenants);
+    if (cfg->tenant_quota_pages) {
+        s->quota = cfg->tenant_quota_pages;
+    } else {
+        uint64_t used = 0;
+        if (pbm_pool_used(pool, &used, nullptr) != PBM_OK) { delete s; return PBM_ERR_CUDA; }
+        const uint64_t cap = (uint64_t)(cfg->max_occupancy * (double)pool->n_pages);
+        s->quota = cap > used ? (cap - used) / cfg->n_tenants : 0;
+    }
+    s->quota = std::min<uint64_t>(s->quota, cfg->ring_pages);
     const size_t ring_total = (size_t)cfg->n_tenants * cfg->ring_pages;
     bool ok = cudaMalloc(&s->d_rings, ring_total * sizeof(int32_t)) == cudaSuccess &&
               cudaMemset(s->d_rings, 0xff, ring_total * sizeof(int32_t)) == cudaSuccess &&
@@ -142,16 +155,12 @@ int pbm_server_run(pbm_server* s, const pbm_request* reqs, uint64_t n, pbm_reque
     for (uint64_t i = 0; i < n; ++i) {
         if (reqs[i].tenant >= s->cfg.n_tenants || reqs[i].op < PBM_REQ_ALLOC || reqs[i].op > PBM_REQ_FETCH)
             return PBM_ERR_INVALID;
-        if (reqs[i].op == PBM_REQ_FETCH && !s->bm) return PBM_ERR_INVALID;
+        if (reqs[i].op == PBM_REQ_FETCH && (!s->bm || reqs[i].count > s->max_fetch)) return PBM_ERR_INVALID;
         if (i && reqs[i].arrival_s < reqs[i - 1].arrival_s) return PBM_ERR_INVALID;
         res[i] = pbm_request_result{};
         res[i].status = -1;
     }
-    uint64_t used0 = 0;
-    int rc = pbm_pool_used(s->pool, &used0, nullptr);
-    if (rc) return rc;
-    const uint64_t cap = (uint64_t)(s->cfg.max_occupancy * (double)s->n_pages);
-    uint64_t held_est = used0;
+    int rc = PBM_OK;
     const uint32_t R = s->cfg.ring_pages;
     const auto t0 = Clock::now();
     auto now_s = [&]() { return std::chrono::duration<double>(Clock::now() - t0).count(); };
@@ -184,8 +193,6 @@ int pbm_server_run(pbm_server* s, const pbm_request* reqs, uint64_t n, pbm_reque
                         tn.completed += tn.allocs.front().pages;
                         tn.allocs.pop_front();
                     }
-                } else if (reqs[r].op == PBM_REQ_FREE) {
-                    held_est -= res[r].pages;
                 }
                 ++finished;
             }
@@ -208,7 +215,14 @@ int pbm_server_run(pbm_server* s, const pbm_request* reqs, uint64_t n, pbm_reque
                     const uint64_t r = tn.queue.front();
                     const pbm_request& q = reqs[r];
                     if (q.op == PBM_REQ_ALLOC) {
-                        if (held_est + q.count > cap || tn.tail - tn.head + q.count > R) break;
+                        if (tn.logical + q.count > s->quota) {   // over budget: rejected, not queued
+                            res[r].status = PBM_ERR_EXHAUSTED;
+                            res[r].admit_s = res[r].done_s = ta;
+                            res[r].pages = 0;
+                            tn.queue.pop_front();
+                            ++finished;
+                            continue;
+                        }
                         const uint64_t pos = tn.tail % R;
                         const uint64_t first = std::min<uint64_t>(q.count, R - pos);
                         slot->h_groups[ng++] = pbm_group{PBM_OP_ALLOC, (uint32_t)first, (uint64_t)ti * R + pos};
@@ -217,7 +231,6 @@ int pbm_server_run(pbm_server* s, const pbm_request* reqs, uint64_t n, pbm_reque
                         tn.tail += q.count;
                         tn.logical += q.count;
                         tn.allocs.push_back(Pending{r, q.count, false});
-                        held_est += q.count;
                         res[r].pages = q.count;
                     } else if (q.op == PBM_REQ_FREE) {
                         const uint64_t k2 = std::min<uint64_t>(q.count, tn.logical);

@@ -117,7 +117,7 @@ class RequestResult(Structure):
 
 class ServerConfig(Structure):
     _fields_ = [("n_tenants", c_uint32), ("ring_pages", c_uint32), ("n_streams", c_uint32),
-                ("max_batch_requests", c_uint32), ("max_fetch_pages", c_uint32), ("reserved", c_uint32),
+                ("max_batch_requests", c_uint32), ("max_fetch_pages", c_uint32), ("tenant_quota_pages", c_uint32),
                 ("max_occupancy", c_double), ("drain_timeout_s", c_double), ("walk", WalkConfig)]
 
 
@@ -471,9 +471,9 @@ class Server:
 
     def __init__(self, pool: Pool, n_tenants, ring_pages, n_streams=4, max_batch_requests=1024,
                  max_occupancy=0.95, drain_timeout_s=2.0, walk=None, bufmgr=None, fetch_pages=None,
-                 max_fetch_pages=0):
+                 max_fetch_pages=0, tenant_quota_pages=0):
         self.lib = lib()
-        cfg = ServerConfig(n_tenants, ring_pages, n_streams, max_batch_requests, max_fetch_pages, 0,
+        cfg = ServerConfig(n_tenants, ring_pages, n_streams, max_batch_requests, max_fetch_pages, tenant_quota_pages,
                            max_occupancy, drain_timeout_s, walk or walk_config())
         h = c_void_p()
         nf = 0 if fetch_pages is None else fetch_pages.numel()

@@ -13,11 +13,9 @@ Every scenario keeps the pool far from exhaustion: the reference traps
 """
 from __future__ import annotations
 
-import ctypes
 import json
 import os
 import sys
-from ctypes import byref, c_int, c_uint, c_uint64, c_void_p
 
 import numpy as np
 
@@ -26,78 +24,7 @@ ROOT = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, os.path.join(ROOT, "oracle"))
 import oracle  # noqa: E402
 
-REF_DIR = os.path.join(ROOT, "oracle", "_ref")
-
-
-class Driver:
-    def __init__(self):
-        self.cu = ctypes.CDLL("libcuda.so.1")
-        self._ck(self.cu.cuInit(0), "cuInit")
-        dev = c_int()
-        self._ck(self.cu.cuDeviceGet(byref(dev), 0), "cuDeviceGet")
-        ctx = c_void_p()
-        self._ck(self.cu.cuDevicePrimaryCtxRetain(byref(ctx), dev), "cuDevicePrimaryCtxRetain")
-        self._ck(self.cu.cuCtxSetCurrent(ctx), "cuCtxSetCurrent")
-        self.allocs = []
-
-    @staticmethod
-    def _ck(rc, what):
-        if rc != 0:
-            raise RuntimeError(f"{what} failed with CUresult {rc}")
-
-    def module(self, name):
-        m = c_void_p()
-        self._ck(self.cu.cuModuleLoad(byref(m), os.path.join(REF_DIR, name).encode()), "cuModuleLoad " + name)
-        return m
-
-    def fn(self, mod, name):
-        f = c_void_p()
-        self._ck(self.cu.cuModuleGetFunction(byref(f), mod, name.encode()), "cuModuleGetFunction " + name)
-        return f
-
-    def alloc(self, nbytes):
-        p = c_uint64()
-        self._ck(self.cu.cuMemAlloc_v2(byref(p), ctypes.c_size_t(max(nbytes, 4))), "cuMemAlloc")
-        self.allocs.append(p.value)
-        return p.value
-
-    def h2d(self, dptr, arr):
-        arr = np.ascontiguousarray(arr)
-        self._ck(self.cu.cuMemcpyHtoD_v2(c_uint64(dptr), arr.ctypes.data_as(c_void_p),
-                                         ctypes.c_size_t(arr.nbytes)), "cuMemcpyHtoD")
-
-    def d2h(self, arr, dptr):
-        self._ck(self.cu.cuMemcpyDtoH_v2(arr.ctypes.data_as(c_void_p), c_uint64(dptr),
-                                         ctypes.c_size_t(arr.nbytes)), "cuMemcpyDtoH")
-        return arr
-
-    def upload(self, arr):
-        arr = np.ascontiguousarray(arr)
-        d = self.alloc(arr.nbytes)
-        self.h2d(d, arr)
-        return d
-
-    def launch(self, f, grid, block, *args):
-        vals = []
-        for a in args:
-            if isinstance(a, tuple):  # ('u64', value) device pointer
-                vals.append(c_uint64(a[1]))
-            elif isinstance(a, np.uint32):
-                vals.append(c_uint(int(a)))
-            else:
-                vals.append(c_int(int(a)))
-        params = (c_void_p * len(vals))(*[ctypes.cast(byref(v), c_void_p) for v in vals])
-        self._ck(self.cu.cuLaunchKernel(f, grid, 1, 1, block, 1, 1, 0, None, params, None), "cuLaunchKernel")
-        self._ck(self.cu.cuCtxSynchronize(), "cuCtxSynchronize")
-
-    def free_all(self):
-        for p in self.allocs:
-            self.cu.cuMemFree_v2(c_uint64(p))
-        self.allocs = []
-
-
-def D(p):
-    return ("u64", p)
+from ref_driver import D, Driver  # noqa: E402
 
 
 def int_map(n_pages, occ, seed):

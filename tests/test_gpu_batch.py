@@ -71,6 +71,37 @@ def test_swap_keeps_occupancy(cuda, pbm_mod, orc, mode, strategy, W, wb):
     pool.close()
 
 
+@pytest.mark.parametrize("fused", [True, False])
+def test_graph_replays_past_its_steps_wrap(cuda, pbm_mod, orc, fused):
+    """A graph of 2 descriptor tables replayed 5 times reads tables 0,1,0,1,0
+    (never past the table), with a fresh seed each replay.  The unfused form
+    (more groups than one block scans) runs its prefix kernel in the graph."""
+    torch = cuda
+    pbm = pbm_mod
+    T, occ, seed = 1 << 20, 0.9, 2
+    n_groups = 64 if fused else 5000
+    pool = pbm.Pool(T, 64)
+    pool.prefill(occ, seed)
+    words, held = _held_arena(orc, T, occ, seed)
+    H = len(held)
+    arena = torch.from_numpy(held).cuda()
+    rng = np.random.default_rng(3)
+    counts = rng.integers(1, 40, size=(2, n_groups))
+    tab = np.concatenate([_descs(counts[s], pbm.OP_SWAP, int(counts[:s].sum()), H) for s in range(2)])
+    d_tab = torch.from_numpy(tab.view(np.uint8).copy()).cuda()
+    g = pool.graph(pbm.walk_config(pbm.COLLAB_RW_BM), d_tab, n_groups, 2, arena, H, 900)
+    for _ in range(5):
+        g.replay()
+    g.close()
+    torch.cuda.synchronize()
+    st = pool.stats()
+    expect = 3 * int(counts[0].sum()) + 2 * int(counts[1].sum())
+    assert st.failures == 0 and st.successes == expect == st.frees
+    chk = pool.check(arena, H)
+    assert chk.n_duplicates == 0 and chk.n_not_marked == 0 and chk.used_pages == H
+    pool.close()
+
+
 def test_alloc_then_free_groups(cuda, pbm_mod, orc):
     """ALLOC groups fill an arena, FREE groups release it; mixed ops in one
     persistent batch keep the invariants and free restores the prefill."""

@@ -270,7 +270,7 @@ def run_ours(args, rank, world, local_rank):
     tuned = pool.autotune(d_tab[:N_GROUPS * 16], N_GROUPS, int(counts[0].sum()), arena, H, seed=SEED0 - 999,
                           reps=4, stream=sh)
     torch.cuda.synchronize()
-    cfg = pbm.walk_config(pbm.COLLAB_RW_BM, word_bits=32, collab_width=32, free_merge=1)
+    cfg = pbm.walk_config(pbm.COLLAB_RW_BM, word_bits=32, collab_width=32, blocks_per_sm=5)
     if tuned:
         cfg = pbm.WalkConfig.from_buffer_copy(tuned[0].cfg)
 
@@ -332,7 +332,7 @@ def run_ours(args, rank, world, local_rank):
     plain_value = sum(2 * int(pairs_per_step[s]) for s, _ in res_plain) / (p_ms * 1e-3)
 
     # ---- per-thread word-probe walk, batched (config-2 comparison) ----
-    cfg_pt = pbm.walk_config(pbm.RANDOM_WALK_BM, word_bits=32, free_merge=1)
+    cfg_pt = pbm.walk_config(pbm.RANDOM_WALK_BM, word_bits=32)
     g_pt = pool.graph(cfg_pt, d_tab, N_GROUPS, n_steps, arena, H, SEED0 + 7777, sh)
     for s in range(args.warmup):
         g_pt.replay(sh)
@@ -610,7 +610,7 @@ def config_buffer_manager(torch, pbm, stream, flush, n_fetch=1 << 26, round_size
     return out
 
 
-def config_malloc(torch, pbm, stream, flush, rounds=16, plain_rounds=4):
+def config_malloc(torch, pbm, stream, flush, rounds=16, plain_rounds=4, max_steps=512):
     """32 GiB pool of 4 KiB pages; per round 256 malloc groups (LogU[1,65536]
     requests, sizes LogU[16 B, 64 KiB] in power-of-two classes, seed 4) and
     frees of a uniformly random 50% of the live blocks, in one launch."""
@@ -622,7 +622,9 @@ def config_malloc(torch, pbm, stream, flush, rounds=16, plain_rounds=4):
     live_cap = 3 * n_max
     gen = torch.Generator(device="cuda")
     out = {"pool_pages": T, "page_size": PAGE_SIZE, "rounds": rounds, "unit": "ops/s",
-           "ops": "mallocs + frees", "l2": "flushed before every round"}
+           "ops": "mallocs + frees", "l2": "flushed before every round", "max_steps": max_steps,
+           "note": "the trace outgrows the pool (about 34 GB live before each round's frees on 32 GiB), "
+                   "so part of every round fails after max_steps jumps"}
     for form in ("graph", "plain"):
         pool = pbm.Pool(T, PAGE_SIZE, materialize=True)
         pool.malloc_init()
@@ -633,7 +635,8 @@ def config_malloc(torch, pbm, stream, flush, rounds=16, plain_rounds=4):
         n_groups = 2 * N_GROUPS
         dt = np.dtype([("op", "<i4"), ("count", "<u4"), ("offset", "<u8")])
         d_tab = torch.zeros(n_groups * 16, dtype=torch.uint8, device="cuda")
-        graph = pool.malloc_graph(d_tab, n_groups, 1, sizes, ptrs, slots, 91, stream=sh) if form == "graph" else None
+        graph = (pool.malloc_graph(d_tab, n_groups, 1, sizes, ptrs, slots, 91, max_steps=max_steps, stream=sh)
+                 if form == "graph" else None)
         live = torch.empty(0, dtype=torch.int64, device="cuda")
         t_ms, ops, fails = 0.0, 0, 0
         nr = rounds if form == "graph" else plain_rounds
@@ -663,7 +666,8 @@ def config_malloc(torch, pbm, stream, flush, rounds=16, plain_rounds=4):
             else:
                 hg = pbm.groups_array([(int(t["op"]), int(t["count"]), int(t["offset"])) for t in tab])
                 t_ms += _ev_ms(torch, stream, lambda: pool.malloc_batch(d_tab, hg, n_groups, sizes, ptrs, slots,
-                                                                        1000 + r, pbm.LAUNCH_PLAIN, stream=sh))
+                                                                        1000 + r, pbm.LAUNCH_PLAIN,
+                                                                        max_steps=max_steps, stream=sh))
             new = ptrs[:n_new]
             ok = new != 0
             fails += n_new - int(ok.sum().item())
@@ -766,7 +770,9 @@ def run_profile_case(args):
     tab = build_descriptors(counts, len(held), pbm.OP_SWAP)
     d_tab = torch.from_numpy(tab.view(np.uint8).reshape(-1).copy()).to(dev)
     flush = torch.empty(512 << 20, dtype=torch.uint8, device=dev)
-    walk = {"collab32": pbm.walk_config(pbm.COLLAB_RW_BM, word_bits=32, collab_width=32),
+    walk = {"collab32c": pbm.walk_config(pbm.COLLAB_RW_BM, word_bits=32, collab_width=32, blocks_per_sm=5,
+                                         free_merge=0),
+            "collab32": pbm.walk_config(pbm.COLLAB_RW_BM, word_bits=32, collab_width=32),
             "collab64": pbm.walk_config(pbm.COLLAB_RW_BM, word_bits=64, collab_width=32),
             "word32": pbm.walk_config(pbm.RANDOM_WALK_BM, word_bits=32)}[args.profile_walk]
     graph = pool.graph(walk, d_tab, N_GROUPS, n_steps, arena, len(held), SEED0, sh)
@@ -801,7 +807,9 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--profile", action="store_true", help="batched form only (for ncu)")
-    ap.add_argument("--profile-walk", default="collab32", choices=["collab32", "collab64", "word32"])
+    ap.add_argument("--profile-walk", default="collab32c", choices=["collab32c", "collab32", "collab64", "word32"],
+                    help="collab32c: collaborative walk, 32-bit words, register-capped 5 blocks/SM, "
+                         "frees unmerged (the autotuner's pick at 90%%)")
     ap.add_argument("--configs", default="all",
                     help="other workloads measured after the headline: all, none, or a comma list of "
                          "claim_write_free_50pct,occupancy_sweep,buffer_manager,malloc,serving")

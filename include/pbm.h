@@ -75,7 +75,8 @@ typedef struct {
     uint32_t stride;        /* words between neighbouring lanes of a collaborating group (>=1) */
     uint32_t max_steps;     /* bound on random jumps per request (0 = 4096) */
     int32_t  block_size;    /* threads per block (0 = 256) */
-    int32_t  blocks_per_sm; /* persistent form: resident blocks per SM (0 = occupancy limit) */
+    int32_t  blocks_per_sm; /* persistent form: resident blocks per SM (0 = occupancy limit;
+                               >= 5 selects the register-capped kernels, 5 blocks) */
     int32_t  free_merge;    /* 1 = merge frees of one word within a warp */
 } pbm_walk_config;
 
@@ -120,7 +121,8 @@ int pbm_pool_prefill_bernoulli(pbm_pool *pool, double occupancy, uint64_t seed, 
 /* getFreePagePercentage() [RandomWalkBasic_BM.cuh:117-145], printNumPagesLeft*():
  * number of held pages (popcount of the bitmap); synchronises `stream`. */
 int pbm_pool_used(pbm_pool *pool, uint64_t *h_used, void *stream);
-/* Snapshot / restore of the bitmap (bytes = bitmap_bytes); synchronous. */
+/* Snapshot / restore of the bitmap (bytes = bitmap_bytes); synchronous.  A
+ * write sets the padding bits past the last page again. */
 int pbm_pool_read_bitmap(pbm_pool *pool, void *h_dst, size_t bytes, void *stream);
 int pbm_pool_write_bitmap(pbm_pool *pool, const void *h_src, size_t bytes, void *stream);
 /* Device addresses of a pool's state, for a caller's own kernels (the
@@ -168,7 +170,20 @@ int pbm_alloc_runs(pbm_pool *pool, uint32_t n, const int32_t *d_npages, uint32_t
                    uint32_t max_steps, int32_t *d_ids, int32_t *d_steps, void *stream);
 int pbm_alloc_runs_serial(pbm_pool *pool, uint32_t n, const int32_t *d_npages, uint32_t seed,
                           uint32_t max_steps, int32_t *d_ids, int32_t *d_steps, void *stream);
-/* [releasePages, CollabRW_BM.cuh:61-71; freeRW, RWMalloc.cuh:329-334] */
+/* Runs of d_npages[i] pages (1 .. 65536) that may cross word boundaries,
+ * which lifts the one-word limit of the reference's contiguous claims: per
+ * jump the walk scans from a random word for a free run reaching across
+ * words (for runs of <= 32 pages also inside one word) and claims it word by
+ * word, releasing its bits again if another claim took part of it.
+ * [getXPage*_BM, parallelPage.cu:934-991, 1104-1142; getNPage, RWMalloc.cuh:113-157,
+ * without their single-word restriction] */
+int pbm_alloc_spans(pbm_pool *pool, uint32_t n, const int32_t *d_npages, uint32_t seed,
+                    uint32_t max_steps, int32_t *d_ids, int32_t *d_steps, void *stream);
+int pbm_alloc_spans_serial(pbm_pool *pool, uint32_t n, const int32_t *d_npages, uint32_t seed,
+                           uint32_t max_steps, int32_t *d_ids, int32_t *d_steps, void *stream);
+/* Releases d_npages[i] pages from d_ids[i] on (1 .. 65536 pages, runs from
+ * either claim form; entries with an id < 0 or past the pool are skipped).
+ * [releasePages, CollabRW_BM.cuh:61-71; freeRW, RWMalloc.cuh:329-334] */
 int pbm_free_runs(pbm_pool *pool, uint32_t n, const int32_t *d_ids, const int32_t *d_npages,
                   void *stream);
 
@@ -239,9 +254,11 @@ int pbm_malloc_counts(pbm_pool *pool, uint64_t *h_live_runs, uint64_t *h_bad_fre
 /* Autotuner (no reference counterpart).  Runs the caller's batch of
  * `requests` swap requests (descriptors in d_groups, all PBM_OP_SWAP) through
  * the persistent kernel for every candidate configuration -- walk, width
- * 8/16/32, 32/64-bit words, stride, blocks per SM, merged frees -- `reps`
- * times each, and returns up to max_out results sorted fastest first.  Swaps
- * keep the pool's occupancy, so tune once per occupancy band. */
+ * 8/16/32, 32/64-bit words, stride, blocks per SM, merged frees -- once
+ * untimed and then `reps` times, each timed alone after an L2 flush (a
+ * 256 MiB device scratch, allocated for the call), ranked by the median
+ * (ms_per_batch), and returns up to max_out results sorted fastest first.
+ * Swaps keep the pool's occupancy, so tune once per occupancy band. */
 typedef struct {
     pbm_walk_config cfg;
     float ms_per_batch;

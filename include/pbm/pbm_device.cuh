@@ -542,6 +542,105 @@ __device__ __forceinline__ int32_t walk_run(const PoolView& v, uint32_t n, int32
 }
 
 // ---------------------------------------------------------------------------
+// Runs that may cross word boundaries (getXPage*_BM / getNPage without the
+// one-word limit of parallelPage.cu:1104-1142 and RWMalloc.cuh:203-248).
+// Per jump the walk scans words w, w+1, ... (at most ceil(n/32) + 1 of them,
+// never past the last word), tracking the free run that reaches the top bit
+// of the previous word: a run is found where that run plus the current
+// word's free low bits reaches n, or -- for n <= 32 -- inside the current
+// word (lowest start).  The run is then claimed word by word with atomicOr;
+// if a word had lost some of its bits to another claim, every bit this claim
+// set is released again and the walk jumps anew.  steps = jumps.
+// ---------------------------------------------------------------------------
+constexpr uint32_t kMaxSpanPages = 1u << 16;
+
+// bits lo..hi (inclusive) of a 32-bit word
+__host__ __device__ __forceinline__ uint32_t bit_range(uint32_t lo, uint32_t hi) {
+    return (hi >= 31u ? kFull32 : ((1u << (hi + 1u)) - 1u)) & ~((1u << lo) - 1u);
+}
+
+// mask of the pages of run [p0, p0+n) that lie in word ww
+__host__ __device__ __forceinline__ uint32_t span_mask(uint32_t p0, uint32_t n, uint32_t ww) {
+    const uint32_t a = p0 >> 5, b = (p0 + n - 1u) >> 5;
+    return bit_range(ww == a ? (p0 & 31u) : 0u, ww == b ? ((p0 + n - 1u) & 31u) : 31u);
+}
+
+// First run of n free pages seen from word w on (-1 if none in the window).
+__device__ __forceinline__ int32_t find_span(const PoolView& v, uint32_t w, uint32_t n) {
+    const uint32_t L = v.n_words32;
+    if (n <= 32u) {
+        // two-word window, both loads in flight together (same result as the loop below)
+        const uint32_t v0 = load_word(v.words + w);
+        const uint32_t v1 = w + 1u < L ? load_word(v.words + w + 1u) : kFull32;
+        uint32_t r = run_starts(~v0, n);
+        if (r) return (int32_t)(w * 32u + (uint32_t)(__ffs((int)r) - 1));
+        const uint32_t hi = v0 ? (uint32_t)__clz((int)v0) : 32u;
+        if (w + 1u >= L) return -1;
+        const uint32_t lo = v1 ? (uint32_t)(__ffs((int)v1) - 1) : 32u;
+        if (hi > 0u && hi + lo >= n) return (int32_t)(w * 32u + 32u - hi);
+        r = run_starts(~v1, n);
+        if (r) return (int32_t)((w + 1u) * 32u + (uint32_t)(__ffs((int)r) - 1));
+        return -1;
+    }
+    const uint32_t nscan = (n + 31u) / 32u + 1u;
+    uint32_t run = 0, start = 0;   // free pages ending at the top of the previous word
+    for (uint32_t k = 0; k < nscan && w + k < L; ++k) {
+        const uint32_t ww = w + k;
+        const uint32_t val = load_word(v.words + ww);
+        const uint32_t lo = val ? (uint32_t)(__ffs((int)val) - 1) : 32u;   // free low bits
+        if (run > 0u && run + lo >= n) return (int32_t)start;
+        if (n <= 32u) {
+            const uint32_t r = run_starts(~val, n);
+            if (r) return (int32_t)(ww * 32u + (uint32_t)(__ffs((int)r) - 1));
+        }
+        if (val == 0u) {
+            if (run == 0u) start = ww * 32u;
+            run += 32u;
+        } else {
+            const uint32_t hi = (uint32_t)__clz((int)val);            // free top bits
+            run = hi;
+            start = ww * 32u + 32u - hi;
+        }
+    }
+    return -1;
+}
+
+__device__ __forceinline__ void free_span(const PoolView& v, int32_t id, uint32_t n) {
+    const uint32_t p0 = (uint32_t)id;
+    for (uint32_t ww = p0 >> 5; ww <= (p0 + n - 1u) >> 5; ++ww) atomicAnd(v.words + ww, ~span_mask(p0, n, ww));
+}
+
+__device__ __forceinline__ int32_t walk_span(const PoolView& v, uint32_t n, int32_t seed0,
+                                             uint32_t max_steps, int32_t* steps_out) {
+    const uint32_t L = v.n_words32;
+    int32_t x = seed0 & 0x7fffffff;   // walks run on 31-bit states
+    uint32_t s = 0;
+    while (s < max_steps) {
+        ++s;
+        x = lcg31(x);
+        const int32_t found = find_span(v, idx_hi(x, L), n);
+        if (found < 0) continue;
+        const uint32_t p0 = (uint32_t)found, a = p0 >> 5, b = (p0 + n - 1u) >> 5;
+        uint32_t ww = a;
+        for (; ww <= b; ++ww) {
+            const uint32_t m = span_mask(p0, n, ww);
+            const uint32_t old = atomicOr(v.words + ww, m);
+            if (old & m) {                                   // lost part of the run
+                if (m & ~old) atomicAnd(v.words + ww, ~(m & ~old));
+                break;
+            }
+        }
+        if (ww > b) {
+            if (steps_out) *steps_out = (int32_t)s;
+            return found;
+        }
+        for (uint32_t k = a; k < ww; ++k) atomicAnd(v.words + k, ~span_mask(p0, n, k));   // roll back
+    }
+    if (steps_out) *steps_out = (int32_t)s;
+    return -1;
+}
+
+// ---------------------------------------------------------------------------
 // FIFO free list (linked-list strategy, parallelPage.cu:342-440, restated
 // lock-free).  get: reserve one free page on `avail`, take a head ticket,
 // exchange the ring slot with -1 (bounded wait for the put that holds the

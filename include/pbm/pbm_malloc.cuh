@@ -6,7 +6,8 @@
 //
 //   * sizes are rounded up to power-of-two classes, 16 B .. 64 KiB;
 //   * requests of at least a page get their own run of size/page_size pages
-//     (at most 32, inside one bitmap word, claimed whole by compare-and-swap);
+//     (walk_span: the run may cross bitmap words, which the reference's
+//     one-word find0Range cannot, RWMalloc.cuh:159-200);
 //   * the sub-page requests of a group of 32 requests are packed into one run,
 //     largest class first, so every sub-page block is aligned to its own size
 //     (blocks of a page or more start on a page boundary);
@@ -82,7 +83,7 @@ __device__ __forceinline__ void* malloc_group(const MallocView& m, uint32_t acti
         int32_t start = -1;
         if ((int)lane == leader) {
             const uint32_t n = (total + page - 1u) >> m.page_shift;
-            start = walk_run(m.pool, n, seed_small, max_steps, &steps);
+            start = walk_span(m.pool, n, seed_small, max_steps, &steps);
             if (start >= 0) malloc_mark_run(m, start, n, __popc(small_mask));
         }
         start = __shfl_sync(active, start, leader);
@@ -97,7 +98,7 @@ __device__ __forceinline__ void* malloc_group(const MallocView& m, uint32_t acti
             if ((int)lane == l) {
                 const uint32_t n = bytes >> m.page_shift;
                 int32_t s = 0;
-                const int32_t start = walk_run(m.pool, n, seed_own, max_steps, &s);
+                const int32_t start = walk_span(m.pool, n, seed_own, max_steps, &s);
                 steps += s;
                 if (start >= 0) {
                     malloc_mark_run(m, start, n, 1);
@@ -109,7 +110,7 @@ __device__ __forceinline__ void* malloc_group(const MallocView& m, uint32_t acti
     } else if (large) {
         const uint32_t n = bytes >> m.page_shift;
         int32_t s = 0;
-        const int32_t start = walk_run(m.pool, n, seed_own, max_steps, &s);
+        const int32_t start = walk_span(m.pool, n, seed_own, max_steps, &s);
         steps += s;
         if (start >= 0) {
             malloc_mark_run(m, start, n, 1);
@@ -143,7 +144,7 @@ __device__ __forceinline__ bool free_group(const MallocView& m, uint32_t active,
         const int32_t k = __popc(peers);
         const int32_t old = atomicSub(m.live + run, k);
         if (old == k) {
-            free_run(m.pool, run, m.len_of[run]);
+            free_span(m.pool, run, m.len_of[run]);
         } else if (old < k) {
             atomicAdd(m.live + run, k);   // double free: undo, report
             ok = false;

@@ -45,6 +45,7 @@ SIGS = [
     ("orc_dist_clock", c_int32, [_P, c_uint32, POINTER(c_uint32), c_uint32, POINTER(c_int32)]),
     ("orc_dist_clock_arm0", c_uint32, [c_uint32, c_uint32, c_uint32]),
     ("orc_walk_run", c_int32, [_P, c_uint32, c_uint32, c_int32, c_uint32, POINTER(c_int32)]),
+    ("orc_walk_span", c_int32, [_P, c_uint32, c_uint32, c_int32, c_uint32, POINTER(c_int32)]),
     ("orc_free_run", None, [_P, c_int32, c_uint32]),
     ("orc_free_page", None, [_P, c_int32]),
     ("orc_ref_rwbasic_get", c_int32, [_P, c_int32, c_int32, c_int16, POINTER(c_int32)]),
@@ -194,6 +195,22 @@ def replay_runs(words, n_pages, npages, S, max_steps=4096):
         k = int(npages[r])
         if 1 <= k <= 32:
             ids[r] = L.orc_walk_run(P(words), n_pages, k, L.orc_seed(S, r), max_steps, ctypes.byref(st))
+            steps[r] = st.value
+    return ids, steps
+
+
+def replay_spans(words, n_pages, npages, S, max_steps=4096):
+    """Serial replay of pbm_alloc_spans: request r claims npages[r] pages
+    (runs may cross words) with seed orc_seed(S, r)."""
+    L = lib()
+    n = len(npages)
+    ids = np.full(n, -1, dtype=np.int32)
+    steps = np.zeros(n, dtype=np.int32)
+    st = c_int32()
+    for r in range(n):
+        k = int(npages[r])
+        if 1 <= k <= 65536:
+            ids[r] = L.orc_walk_span(P(words), n_pages, k, L.orc_seed(S, r), max_steps, ctypes.byref(st))
             steps[r] = st.value
     return ids, steps
 

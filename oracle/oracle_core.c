@@ -52,6 +52,7 @@ uint32_t orc_shl32(uint32_t x, uint32_t n) { return n >= 32u ? 0u : (x << n); }
 static inline int popc32(uint32_t x) { return __builtin_popcount(x); }
 static inline int popc64(uint64_t x) { return __builtin_popcountll(x); }
 static inline int ctz32(uint32_t x) { return __builtin_ctz(x); }
+static inline int clz32(uint32_t x) { return __builtin_clz(x); }
 static inline int ctz64(uint64_t x) { return __builtin_ctzll(x); }
 
 /* lowest k set bits of m */
@@ -337,10 +338,64 @@ int32_t orc_walk_run(uint32_t *words, uint32_t n_pages, uint32_t n, int32_t seed
     return -1;
 }
 
+static uint32_t bit_range(uint32_t lo, uint32_t hi) {
+    return (hi >= 31u ? ~0u : ((1u << (hi + 1u)) - 1u)) & ~((1u << lo) - 1u);
+}
+
+static uint32_t span_mask(uint32_t p0, uint32_t n, uint32_t ww) {
+    const uint32_t a = p0 >> 5, b = (p0 + n - 1u) >> 5;
+    return bit_range(ww == a ? (p0 & 31u) : 0u, ww == b ? ((p0 + n - 1u) & 31u) : 31u);
+}
+
+/* Releases n contiguous pages from page id on; the run may cross words. */
 void orc_free_run(uint32_t *words, int32_t id, uint32_t n) {
-    uint32_t w = (uint32_t)id >> 5, st = (uint32_t)id & 31u;
-    uint32_t m = (n >= 32u ? ~0u : ((1u << n) - 1u)) << st;
-    words[w] &= ~m;
+    const uint32_t p0 = (uint32_t)id;
+    for (uint32_t ww = p0 >> 5; ww <= (p0 + n - 1u) >> 5; ++ww) words[ww] &= ~span_mask(p0, n, ww);
+}
+
+/* First run of n free pages seen from word w on, scanning at most
+ * ceil(n/32) + 1 words and never past the last one (-1 if none). */
+static int32_t find_span(const uint32_t *words, uint32_t L, uint32_t w, uint32_t n) {
+    const uint32_t nscan = (n + 31u) / 32u + 1u;
+    uint32_t run = 0, start = 0;
+    for (uint32_t k = 0; k < nscan && w + k < L; ++k) {
+        const uint32_t ww = w + k;
+        const uint32_t val = words[ww];
+        const uint32_t lo = val ? (uint32_t)ctz32(val) : 32u;
+        if (run > 0u && run + lo >= n) return (int32_t)start;
+        if (n <= 32u) {
+            const uint32_t r = run_starts(~val, n);
+            if (r) return (int32_t)(ww * 32u + (uint32_t)ctz32(r));
+        }
+        if (val == 0u) {
+            if (run == 0u) start = ww * 32u;
+            run += 32u;
+        } else {
+            const uint32_t hi = (uint32_t)clz32(val);
+            run = hi;
+            start = ww * 32u + 32u - hi;
+        }
+    }
+    return -1;
+}
+
+int32_t orc_walk_span(uint32_t *words, uint32_t n_pages, uint32_t n, int32_t seed0,
+                      uint32_t max_steps, int32_t *steps) {
+    const uint32_t L = (uint32_t)((n_pages + 31u) / 32u);
+    int32_t x = seed0;
+    uint32_t s = 0;
+    while (s < max_steps) {
+        ++s;
+        x = orc_lcg(x);
+        const int32_t found = find_span(words, L, orc_idx_hi(x, L), n);
+        if (found < 0) continue;
+        const uint32_t p0 = (uint32_t)found;
+        for (uint32_t ww = p0 >> 5; ww <= (p0 + n - 1u) >> 5; ++ww) words[ww] |= span_mask(p0, n, ww);
+        if (steps) *steps = (int32_t)s;
+        return found;
+    }
+    if (steps) *steps = (int32_t)s;
+    return -1;
 }
 
 void orc_free_page(uint32_t *words, int32_t id) {

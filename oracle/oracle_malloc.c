@@ -51,7 +51,7 @@ void orc_malloc_group(orc_malloc_t *m, const uint64_t *sizes, int lanes, int32_t
     if (leader >= 0) {
         const uint32_t n = (total + page - 1u) >> m->page_shift;
         int32_t s = 0;
-        int32_t start = orc_walk_run(m->words, m->n_pages, n, seed_small, max_steps, &s);
+        int32_t start = orc_walk_span(m->words, m->n_pages, n, seed_small, max_steps, &s);
         steps[leader] += s;
         if (start >= 0) {
             mark_run(m, start, n, n_small);
@@ -63,7 +63,7 @@ void orc_malloc_group(orc_malloc_t *m, const uint64_t *sizes, int lanes, int32_t
         if (!large[l]) continue;
         const uint32_t n = bytes[l] >> m->page_shift;
         int32_t s = 0;
-        int32_t start = orc_walk_run(m->words, m->n_pages, n, seed_own[l], max_steps, &s);
+        int32_t start = orc_walk_span(m->words, m->n_pages, n, seed_own[l], max_steps, &s);
         steps[l] += s;
         if (start >= 0) {
             mark_run(m, start, n, 1);

@@ -150,7 +150,13 @@ uint32_t orc_dist_clock_arm0(uint32_t S, uint32_t slot, uint32_t n_pages);
 int32_t orc_walk_run(uint32_t *words, uint32_t n_pages, uint32_t n, int32_t seed0,
                      uint32_t max_steps, int32_t *steps);
 
-/* Release n contiguous pages starting at page id (same word). */
+/* Contiguous run of n pages (1 <= n <= 65536) that may cross word
+ * boundaries: per jump, scan from a random word for a run reaching across
+ * words (or, for n <= 32, inside one word); the first one found is taken. */
+int32_t orc_walk_span(uint32_t *words, uint32_t n_pages, uint32_t n, int32_t seed0,
+                      uint32_t max_steps, int32_t *steps);
+
+/* Release n contiguous pages starting at page id (the run may cross words). */
 void orc_free_run(uint32_t *words, int32_t id, uint32_t n);
 void orc_free_page(uint32_t *words, int32_t id);
 

@@ -34,27 +34,7 @@ struct Acc {
 };
 
 __device__ __forceinline__ void flush_acc(const Acc& a, DevStats* st) {
-    __shared__ unsigned long long sh[3];
-    if (threadIdx.x == 0) { sh[0] = 0; sh[1] = 0; sh[2] = 0; }
-    __syncthreads();
-    unsigned long long ok = a.ok, fail = a.fail, steps = a.steps;
-#pragma unroll
-    for (int d = 16; d > 0; d >>= 1) {
-        ok += __shfl_down_sync(0xffffffffu, ok, d);
-        fail += __shfl_down_sync(0xffffffffu, fail, d);
-        steps += __shfl_down_sync(0xffffffffu, steps, d);
-    }
-    if ((threadIdx.x & 31) == 0) {
-        if (ok) atomicAdd(&sh[0], ok);
-        if (fail) atomicAdd(&sh[1], fail);
-        if (steps) atomicAdd(&sh[2], steps);
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        if (sh[0]) atomicAdd(&st->successes, sh[0]);
-        if (sh[1]) atomicAdd(&st->failures, sh[1]);
-        if (sh[2]) atomicAdd(&st->steps, sh[2]);
-    }
+    block_add_counters<3>({a.ok, a.fail, a.steps}, {&st->successes, &st->failures, &st->steps});
 }
 
 enum class Walk { Page, Word32, Word64, Crw, SingleClock, DistClock };
@@ -96,12 +76,7 @@ __global__ void __launch_bounds__(256) k_alloc_thread(AllocArgs a) {
         acc.fail += id < 0;
         acc.steps += (unsigned long long)s;
     }
-    if (blockDim.x >= 32) flush_acc(acc, a.stats);
-    else if (acc.ok + acc.fail) {
-        atomicAdd(&a.stats->successes, acc.ok);
-        atomicAdd(&a.stats->failures, acc.fail);
-        atomicAdd(&a.stats->steps, acc.steps);
-    }
+    flush_acc(acc, a.stats);
 }
 
 // Warp-collaborative walk: groups of W lanes take W consecutive requests.
@@ -132,12 +107,7 @@ __global__ void __launch_bounds__(256) k_alloc_collab(AllocArgs a) {
             acc.steps += (unsigned long long)s;
         }
     }
-    if (blockDim.x >= 32) flush_acc(acc, a.stats);
-    else if (acc.ok + acc.fail) {
-        atomicAdd(&a.stats->successes, acc.ok);
-        atomicAdd(&a.stats->failures, acc.fail);
-        atomicAdd(&a.stats->steps, acc.steps);
-    }
+    flush_acc(acc, a.stats);
 }
 
 __global__ void __launch_bounds__(256) k_fifo_alloc(AllocArgs a, FifoState* st, int32_t* ring) {
@@ -153,25 +123,7 @@ __global__ void __launch_bounds__(256) k_fifo_alloc(AllocArgs a, FifoState* st, 
         acc.fail += id < 0;
         acc.steps += (unsigned long long)s;
     }
-    if (blockDim.x >= 32) {
-        // trip counts differ across lanes here; reduce through shared atomics
-        __shared__ unsigned long long sh[3];
-        if (threadIdx.x == 0) { sh[0] = sh[1] = sh[2] = 0; }
-        __syncthreads();
-        if (acc.ok) atomicAdd(&sh[0], acc.ok);
-        if (acc.fail) atomicAdd(&sh[1], acc.fail);
-        if (acc.steps) atomicAdd(&sh[2], acc.steps);
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            if (sh[0]) atomicAdd(&a.stats->successes, sh[0]);
-            if (sh[1]) atomicAdd(&a.stats->failures, sh[1]);
-            if (sh[2]) atomicAdd(&a.stats->steps, sh[2]);
-        }
-    } else if (acc.ok + acc.fail) {
-        atomicAdd(&a.stats->successes, acc.ok);
-        atomicAdd(&a.stats->failures, acc.fail);
-        atomicAdd(&a.stats->steps, acc.steps);
-    }
+    flush_acc(acc, a.stats);
 }
 
 __global__ void __launch_bounds__(256) k_fifo_free(PoolView v, uint32_t n, const int32_t* ids,
@@ -182,7 +134,7 @@ __global__ void __launch_bounds__(256) k_fifo_free(PoolView v, uint32_t n, const
         if (id < 0 || (uint32_t)id >= v.n_pages) continue;
         if (fifo_put(v, st, ring, stats, id)) ++f;
     }
-    if (f) atomicAdd(&stats->frees, f);
+    block_add_counters<1>({f}, {&stats->frees});
 }
 
 // ---- frees ----
@@ -202,27 +154,31 @@ __global__ void __launch_bounds__(256) k_free_pages(PoolView v, uint32_t n, cons
         }
         f += id >= 0;
     }
-    if (f) atomicAdd(&stats->frees, f);
+    block_add_counters<1>({f}, {&stats->frees});
 }
 
 // ---- contiguous runs ----
+// SPAN: runs may cross word boundaries (1 <= k <= kMaxSpanPages); else one
+// word holds the run (1 <= k <= 32, the reference's getXPage semantics).
+template <bool SPAN>
 __global__ void __launch_bounds__(256) k_alloc_runs(AllocArgs a, const int32_t* npages) {
     Acc acc;
     for (uint32_t r = blockIdx.x * blockDim.x + threadIdx.x; r < a.n; r += gridDim.x * blockDim.x) {
         int32_t k = npages[r];
         int32_t s = 0, id = -1;
-        if (k >= 1 && k <= 32) id = walk_run(a.v, (uint32_t)k, request_seed(a.seed, r), a.max_steps, &s);
+        if (SPAN) {
+            if (k >= 1 && (uint32_t)k <= kMaxSpanPages)
+                id = walk_span(a.v, (uint32_t)k, request_seed(a.seed, r), a.max_steps, &s);
+        } else if (k >= 1 && k <= 32) {
+            id = walk_run(a.v, (uint32_t)k, request_seed(a.seed, r), a.max_steps, &s);
+        }
         a.ids[r] = id;
         if (a.steps) a.steps[r] = s;
         acc.ok += id >= 0;
         acc.fail += id < 0;
         acc.steps += (unsigned long long)s;
     }
-    if (acc.ok + acc.fail) {
-        atomicAdd(&a.stats->successes, acc.ok);
-        atomicAdd(&a.stats->failures, acc.fail);
-        atomicAdd(&a.stats->steps, acc.steps);
-    }
+    flush_acc(acc, a.stats);
 }
 
 __global__ void __launch_bounds__(256) k_free_runs(PoolView v, uint32_t n, const int32_t* ids,
@@ -230,11 +186,12 @@ __global__ void __launch_bounds__(256) k_free_runs(PoolView v, uint32_t n, const
     unsigned long long f = 0;
     for (uint32_t r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x) {
         int32_t id = ids[r], k = npages[r];
-        if (id < 0 || (uint32_t)id >= v.n_pages || k < 1 || k > 32 || ((id & 31) + k) > 32) continue;
-        free_run(v, id, (uint32_t)k);
+        if (id < 0 || k < 1 || (uint32_t)k > kMaxSpanPages || (unsigned long long)id + (uint32_t)k > v.n_pages)
+            continue;
+        free_span(v, id, (uint32_t)k);
         f += (unsigned long long)k;
     }
-    if (f) atomicAdd(&stats->frees, f);
+    block_add_counters<1>({f}, {&stats->frees});
 }
 
 // ---- config-1 step: claim one page, write the payload, free ----
@@ -259,12 +216,8 @@ __global__ void __launch_bounds__(256) k_claim_write_free(AllocArgs a, uint32_t 
         acc.fail += id < 0;
         acc.steps += (unsigned long long)s;
     }
-    if (acc.ok + acc.fail) {
-        atomicAdd(&a.stats->successes, acc.ok);
-        atomicAdd(&a.stats->failures, acc.fail);
-        atomicAdd(&a.stats->steps, acc.steps);
-    }
-    if (frees) atomicAdd(&a.stats->frees, frees);
+    block_add_counters<4>({acc.ok, acc.fail, acc.steps, frees},
+                          {&a.stats->successes, &a.stats->failures, &a.stats->steps, &a.stats->frees});
 }
 
 __global__ void k_gather_pages(PoolView v, const int32_t* ids, uint32_t n, uint32_t words_per_page,
@@ -422,7 +375,7 @@ int pbm_free(pbm_pool* pool, const pbm_walk_config* cfg, uint32_t n, const int32
 
 static int alloc_runs_impl(pbm_pool* pool, uint32_t n, const int32_t* d_npages, uint32_t seed,
                            uint32_t max_steps, int32_t* d_ids, int32_t* d_steps, bool serial,
-                           void* stream) {
+                           bool span, void* stream) {
     if (!pool || (n && (!d_ids || !d_npages))) return PBM_ERR_INVALID;
     if (n == 0) return PBM_OK;
     pbm_walk_config c{};
@@ -431,7 +384,8 @@ static int alloc_runs_impl(pbm_pool* pool, uint32_t n, const int32_t* d_npages, 
     AllocArgs a = make_args(pool, &c, n, seed, d_ids, d_steps);
     int block = serial ? 1 : kDefaultBlock;
     int grid = serial ? 1 : (int)((n + (uint32_t)block - 1u) / (uint32_t)block);
-    k_alloc_runs<<<grid, block, 0, (cudaStream_t)stream>>>(a, d_npages);
+    if (span) k_alloc_runs<true><<<grid, block, 0, (cudaStream_t)stream>>>(a, d_npages);
+    else k_alloc_runs<false><<<grid, block, 0, (cudaStream_t)stream>>>(a, d_npages);
     PBM_LAUNCH_CHECK();
     pool->fifo_valid = false;
     return PBM_OK;
@@ -439,12 +393,22 @@ static int alloc_runs_impl(pbm_pool* pool, uint32_t n, const int32_t* d_npages, 
 
 int pbm_alloc_runs(pbm_pool* pool, uint32_t n, const int32_t* d_npages, uint32_t seed,
                    uint32_t max_steps, int32_t* d_ids, int32_t* d_steps, void* stream) {
-    return alloc_runs_impl(pool, n, d_npages, seed, max_steps, d_ids, d_steps, false, stream);
+    return alloc_runs_impl(pool, n, d_npages, seed, max_steps, d_ids, d_steps, false, false, stream);
 }
 
 int pbm_alloc_runs_serial(pbm_pool* pool, uint32_t n, const int32_t* d_npages, uint32_t seed,
                           uint32_t max_steps, int32_t* d_ids, int32_t* d_steps, void* stream) {
-    return alloc_runs_impl(pool, n, d_npages, seed, max_steps, d_ids, d_steps, true, stream);
+    return alloc_runs_impl(pool, n, d_npages, seed, max_steps, d_ids, d_steps, true, false, stream);
+}
+
+int pbm_alloc_spans(pbm_pool* pool, uint32_t n, const int32_t* d_npages, uint32_t seed,
+                    uint32_t max_steps, int32_t* d_ids, int32_t* d_steps, void* stream) {
+    return alloc_runs_impl(pool, n, d_npages, seed, max_steps, d_ids, d_steps, false, true, stream);
+}
+
+int pbm_alloc_spans_serial(pbm_pool* pool, uint32_t n, const int32_t* d_npages, uint32_t seed,
+                           uint32_t max_steps, int32_t* d_ids, int32_t* d_steps, void* stream) {
+    return alloc_runs_impl(pool, n, d_npages, seed, max_steps, d_ids, d_steps, true, true, stream);
 }
 
 int pbm_free_runs(pbm_pool* pool, uint32_t n, const int32_t* d_ids, const int32_t* d_npages, void* stream) {

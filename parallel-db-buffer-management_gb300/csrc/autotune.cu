@@ -3,10 +3,13 @@
 // The sweep covers the walk (per-thread page probe, per-thread word probe,
 // warp-collaborative), the collaboration width (8 / 16 / 32 lanes), 32- vs
 // 64-bit bitmap words, the walk stride between a group's lanes, and blocks
-// per SM (occupancy-limited, or register-capped at 6), and merged frees.  Every candidate
-// runs the caller's own batch of swap requests through the persistent kernel
-// `reps` times, timed with CUDA events; a swap frees one page for every page
-// it takes, so the pool stays in its occupancy band while it is tuned.  The
+// per SM (occupancy-limited, or register-capped at kCappedBlocks), and merged
+// frees.  Every candidate runs the caller's own batch of swap requests through
+// the persistent kernel once untimed and then `reps` times, each timed alone
+// with CUDA events after the L2 is flushed (a 256 MiB write, twice the L2), as
+// a batch that arrives after other work would find it; the median time
+// ranks the candidate.  A swap frees one page for every page it takes, so the
+// pool stays in its occupancy band while it is tuned.  The
 // caller tunes once per band (e.g. after prefilling to 50/75/90/95%) and keeps
 // the winning configuration per band.
 #include <algorithm>
@@ -24,13 +27,13 @@ std::vector<pbm_walk_config> candidates(uint32_t max_steps) {
         pbm_walk_config c{};
         c.max_steps = max_steps;
         c.block_size = 256;
-        c.free_merge = 1;
+        c.free_merge = 0;
         c.stride = 1;
         c.word_bits = 32;
         c.collab_width = 32;
         return c;
     };
-    for (int bps : {0, 6}) {
+    for (int bps : {0, kCappedBlocks}) {
         pbm_walk_config c = base();
         c.strategy = PBM_RANDOM_WALK;
         c.blocks_per_sm = bps;
@@ -55,10 +58,13 @@ std::vector<pbm_walk_config> candidates(uint32_t max_steps) {
                 }
     }
     // the free-merge knob on the default collaborative configuration
-    pbm_walk_config c = base();
-    c.strategy = PBM_COLLAB_RW_BM;
-    c.free_merge = 0;
-    out.push_back(c);
+    for (int bps : {0, kCappedBlocks}) {
+        pbm_walk_config c = base();
+        c.strategy = PBM_COLLAB_RW_BM;
+        c.blocks_per_sm = bps;
+        c.free_merge = 1;
+        out.push_back(c);
+    }
     return out;
 }
 
@@ -72,33 +78,52 @@ extern "C" int pbm_autotune(pbm_pool* pool, const pbm_group* d_groups, uint32_t 
     cudaStream_t s = (cudaStream_t)stream;
     std::vector<pbm_walk_config> cands = candidates(max_steps ? max_steps : kDefaultMaxSteps);
     std::vector<pbm_tune_result> res;
-    cudaEvent_t e0, e1;
-    PBM_CUDA_TRY(cudaEventCreate(&e0));
-    PBM_CUDA_TRY(cudaEventCreate(&e1));
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    void* flush = nullptr;
+    const size_t flush_bytes = size_t(256) << 20;
+    if (cudaMalloc(&flush, flush_bytes) != cudaSuccess) {   // tune without flushes rather than fail
+        cudaGetLastError();
+        flush = nullptr;
+    }
+    auto cleanup = [&]() {
+        if (e0) cudaEventDestroy(e0);
+        if (e1) cudaEventDestroy(e1);
+        if (flush) cudaFree(flush);
+    };
+    if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) {
+        cudaGetLastError();
+        cleanup();
+        return PBM_ERR_CUDA;
+    }
     uint32_t sd = seed;
+    std::vector<float> times((size_t)reps);
+    int rc = PBM_OK;
     for (const pbm_walk_config& c : cands) {
-        // one untimed launch (first-use costs), then `reps` timed launches
-        int rc = pbm_batch_launch(pool, &c, d_groups, nullptr, n_groups, d_arena, arena_len, sd++, nullptr,
-                                  PBM_LAUNCH_PERSISTENT, s);
-        if (rc == PBM_ERR_UNSUPPORTED) continue;
-        if (rc) { cudaEventDestroy(e0); cudaEventDestroy(e1); return rc; }
-        PBM_CUDA_TRY(cudaEventRecord(e0, s));
-        for (int r = 0; r < reps && rc == PBM_OK; ++r)
-            rc = pbm_batch_launch(pool, &c, d_groups, nullptr, n_groups, d_arena, arena_len, sd++, nullptr,
-                                  PBM_LAUNCH_PERSISTENT, s);
-        if (rc) { cudaEventDestroy(e0); cudaEventDestroy(e1); return rc; }
-        PBM_CUDA_TRY(cudaEventRecord(e1, s));
-        PBM_CUDA_TRY(cudaEventSynchronize(e1));
-        float ms = 0.f;
-        PBM_CUDA_TRY(cudaEventElapsedTime(&ms, e0, e1));
+        // one untimed launch (first-use costs), then `reps` launches, each timed after an L2 flush
+        rc = pbm_batch_launch(pool, &c, d_groups, nullptr, n_groups, d_arena, arena_len, sd++, nullptr,
+                              PBM_LAUNCH_PERSISTENT, s);
+        if (rc == PBM_ERR_UNSUPPORTED) { rc = PBM_OK; continue; }
+        for (int r = 0; r < reps && rc == PBM_OK; ++r) {
+            if (flush && cudaMemsetAsync(flush, r & 0xff, flush_bytes, s) != cudaSuccess) rc = PBM_ERR_CUDA;
+            if (!rc && cudaEventRecord(e0, s) != cudaSuccess) rc = PBM_ERR_CUDA;
+            if (!rc) rc = pbm_batch_launch(pool, &c, d_groups, nullptr, n_groups, d_arena, arena_len, sd++, nullptr,
+                                           PBM_LAUNCH_PERSISTENT, s);
+            if (!rc && (cudaEventRecord(e1, s) != cudaSuccess || cudaEventSynchronize(e1) != cudaSuccess ||
+                        cudaEventElapsedTime(&times[(size_t)r], e0, e1) != cudaSuccess))
+                rc = PBM_ERR_CUDA;
+        }
+        if (rc) break;
+        std::sort(times.begin(), times.end());
+        const float ms = times[(size_t)reps / 2];
         pbm_tune_result t{};
         t.cfg = c;
-        t.ms_per_batch = ms / (float)reps;
-        t.ops_per_s = ms > 0.f ? 2.0 * (double)requests * reps / (ms * 1e-3) : 0.0;
+        t.ms_per_batch = ms;
+        t.ops_per_s = ms > 0.f ? 2.0 * (double)requests / (ms * 1e-3) : 0.0;
         res.push_back(t);
     }
-    cudaEventDestroy(e0);
-    cudaEventDestroy(e1);
+    if (rc == PBM_ERR_CUDA) cudaGetLastError();
+    cleanup();
+    if (rc) return rc;
     std::sort(res.begin(), res.end(),
               [](const pbm_tune_result& a, const pbm_tune_result& b) { return a.ops_per_s > b.ops_per_s; });
     const uint32_t n = (uint32_t)std::min<size_t>(res.size(), max_out);

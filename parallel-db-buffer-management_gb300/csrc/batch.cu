@@ -120,16 +120,29 @@ __device__ __forceinline__ unsigned long long wrap_slot(unsigned long long slot,
     return slot;
 }
 
-__device__ __forceinline__ void prefetch_l2(const void* p) {
-    asm volatile("prefetch.global.L2 [%0];" ::"l"(p));
+// Last g in [lo, n_groups) with prefix[g] <= q (prefix[lo] <= q), searched
+// by the whole warp: 32 evenly spaced probes and a ballot narrow the range
+// 32-fold per round (two rounds for 256 groups).
+__device__ __forceinline__ uint32_t find_group_warp(const unsigned long long* prefix, uint32_t n_groups,
+                                                    unsigned long long q, uint32_t lo) {
+    const uint32_t lane = threadIdx.x & 31u;
+    uint32_t hi = n_groups;
+    while (hi - lo > 1u) {
+        const uint32_t stride = (hi - lo + 31u) >> 5;
+        const uint32_t idx = lo + lane * stride;
+        const uint32_t b = __ballot_sync(0xffffffffu, idx < hi && prefix[idx] <= q);
+        lo += (31u - (uint32_t)__clz((int)b)) * stride;
+        hi = min(hi, lo + stride);
+    }
+    return lo;
 }
 
 // The persistent batch kernel.  With a.fuse each block scans the step's
 // group counts into shared memory itself (no separate prefix kernel); with
 // a.done the last block to finish advances the graph's step counter (no
-// separate step kernel), so one graph replay is one launch.  While a chunk is
-// processed, lane 0 prefetches into L2 the next chunk's arena slots and the
-// first bitmap line its walk will read.
+// separate step kernel), so one graph replay is one launch.  (Prefetching the
+// next chunk's arena slots and bitmap line into L2 was measured slower: the
+// extra instructions cost more than the latency they hid.)
 template <BWalk K, int W, typename Word, int MINB>
 __global__ void __launch_bounds__(256, MINB) k_batch_persistent(BatchArgs a) {
     extern __shared__ unsigned long long s_prefix[];
@@ -152,31 +165,15 @@ __global__ void __launch_bounds__(256, MINB) k_batch_persistent(BatchArgs a) {
     volatile int32_t* gslots = slots + (threadIdx.x & ~(uint32_t)(W - 1));
     const unsigned long long warp0 = ((unsigned long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const unsigned long long nwarps = ((unsigned long long)gridDim.x * blockDim.x) >> 5;
-    uint32_t g_next = 0xffffffffu;     // lane 0: group of the next chunk, found while prefetching
+    uint32_t g_next = 0xffffffffu;     // group of the warp's next chunk
     for (unsigned long long chunk = warp0; chunk * 32ull < total; chunk += nwarps) {
         const unsigned long long q0 = chunk * 32ull;
         const unsigned long long q = q0 + lane;
         const bool active = q < total;
-        // group of the chunk's first request: one lane searches, the warp shares
-        uint32_t g0 = 0;
-        if (lane == 0) {
-            g0 = g_next != 0xffffffffu ? g_next : find_group_any(pre, a.n_groups, q0, 0u);
-            const unsigned long long nq0 = q0 + nwarps * 32ull;
-            if (nq0 < total) {
-                const uint32_t ng = find_group_any(pre, a.n_groups, nq0, g0);
-                g_next = ng;
-                const unsigned long long ns = wrap_slot(groups[ng].offset + (nq0 - pre[ng]), a.arena_len);
-                prefetch_l2(a.arena + ns);
-                prefetch_l2(a.arena + wrap_slot(ns + 31ull, a.arena_len));
-                if (K == BWalk::Collab) {
-                    const uint32_t w0 = idx_hi(lcg31(request_seed(seed, (uint32_t)nq0)), L);
-                    const Word* wp = reinterpret_cast<const Word*>(a.v.words);
-                    prefetch_l2(wp + w0);
-                    prefetch_l2(wp + (w0 + 31u < L ? w0 + 31u : w0 + 31u - L));
-                }
-            }
-        }
-        g0 = __shfl_sync(0xffffffffu, g0, 0);
+        // group of the chunk's first request, found by the whole warp while it
+        // handled the previous chunk (chunks of a warp are nwarps*32 apart)
+        const uint32_t g0 = g_next != 0xffffffffu ? g_next : find_group_warp(pre, a.n_groups, q0, 0u);
+        if (q0 + nwarps * 32ull < total) g_next = find_group_warp(pre, a.n_groups, q0 + nwarps * 32ull, g0);
         const unsigned long long g0_end = pre[g0 + 1u];
         int op = PBM_OP_ALLOC;
         unsigned long long slot = 0;
@@ -251,15 +248,18 @@ int persistent_blocks_per_sm(int block) {
 }
 
 // blocks_per_sm <= 0: uncapped registers, as many blocks as fit;
-// 1..5: uncapped registers, that many blocks; >= 6: register-capped variant.
+// 1..kCappedBlocks-1: uncapped registers, that many blocks;
+// >= kCappedBlocks: the variant whose registers are capped for kCappedBlocks
+// resident blocks (5 x 256 threads: at most 51 registers, no spills for the
+// collaborative walk on 32-bit words).
 template <BWalk K, int W, typename Word>
 int launch_batch_kw(const BatchArgs& a, bool persistent, int block, int blocks_per_sm, cudaStream_t s) {
     if (persistent) {
         const size_t smem = a.fuse ? sizeof(unsigned long long) * (a.n_groups + 1u) : 0u;
-        if (blocks_per_sm >= 6) {
-            int fit = persistent_blocks_per_sm<K, W, Word, 6>(block);
+        if (blocks_per_sm >= kCappedBlocks) {
+            int fit = persistent_blocks_per_sm<K, W, Word, kCappedBlocks>(block);
             int per_sm = blocks_per_sm < fit ? blocks_per_sm : fit;
-            k_batch_persistent<K, W, Word, 6><<<sm_count() * per_sm, block, smem, s>>>(a);
+            k_batch_persistent<K, W, Word, kCappedBlocks><<<sm_count() * per_sm, block, smem, s>>>(a);
         } else {
             int fit = persistent_blocks_per_sm<K, W, Word, 1>(block);
             int per_sm = (blocks_per_sm > 0 && blocks_per_sm < fit) ? blocks_per_sm : fit;
@@ -304,12 +304,13 @@ int launch_batch(const pbm_walk_config* c, const BatchArgs& a, bool persistent, 
 int resolve_blocks_per_sm(const pbm_walk_config* c) {
     const int block = c->block_size ? c->block_size : kDefaultBlock;
     const bool w64 = c->word_bits == 64;
-    const bool capped = c->blocks_per_sm >= 6;
-    auto pick = [&](int fit1, int fit6) {
-        if (capped) return c->blocks_per_sm < fit6 ? c->blocks_per_sm : fit6;
+    const bool capped = c->blocks_per_sm >= kCappedBlocks;
+    auto pick = [&](int fit1, int fitc) {
+        if (capped) return c->blocks_per_sm < fitc ? c->blocks_per_sm : fitc;
         return (c->blocks_per_sm > 0 && c->blocks_per_sm < fit1) ? c->blocks_per_sm : fit1;
     };
-#define PBM_FITS(K, W, T) pick(persistent_blocks_per_sm<K, W, T, 1>(block), persistent_blocks_per_sm<K, W, T, 6>(block))
+#define PBM_FITS(K, W, T) \
+    pick(persistent_blocks_per_sm<K, W, T, 1>(block), persistent_blocks_per_sm<K, W, T, kCappedBlocks>(block))
     switch (c->strategy) {
     case PBM_RANDOM_WALK: return PBM_FITS(BWalk::Page, 32, uint32_t);
     case PBM_RANDOM_WALK_BM:

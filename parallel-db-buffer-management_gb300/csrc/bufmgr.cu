@@ -205,13 +205,9 @@ __global__ void __launch_bounds__(256) k_round(BmView b, const int32_t* release_
             if (i < n) frames_out[i] = f;
         }
     }
-    if (ok) atomicAdd(&b.stats->unpins, ok);
-    if (bad) atomicAdd(&b.stats->bad_unpins, bad);
-    if (acc.hits) atomicAdd(&b.stats->hits, acc.hits);
-    if (acc.misses) atomicAdd(&b.stats->misses, acc.misses);
-    if (acc.evictions) atomicAdd(&b.stats->evictions, acc.evictions);
-    if (acc.failures) atomicAdd(&b.stats->failures, acc.failures);
-    if (acc.timeouts) atomicAdd(&b.stats->timeouts, acc.timeouts);
+    block_add_counters<7>({ok, bad, acc.hits, acc.misses, acc.evictions, acc.failures, acc.timeouts},
+                          {&b.stats->unpins, &b.stats->bad_unpins, &b.stats->hits, &b.stats->misses,
+                           &b.stats->evictions, &b.stats->failures, &b.stats->timeouts});
 }
 
 __global__ void k_bm_init(BmView b) {

@@ -21,7 +21,36 @@ inline void count_launch(unsigned long long n = 1) { g_launches.fetch_add(n, std
 int sm_count();
 
 constexpr uint32_t kDefaultMaxSteps = 4096;
+
+// Adds every thread's N counters to dst[0..N) with one global atomic per
+// counter per block: warp shuffles, then one shared atomic per warp.  Every
+// thread of the block calls it (after its loop, converged); blocks whose size
+// is not a multiple of 32 (one-thread replays) add directly.  Per-thread
+// atomics on a shared counter would serialise on one L2 address (~1.5 G/s).
+template <int N>
+__device__ __forceinline__ void block_add_counters(const unsigned long long (&v)[N],
+                                                   unsigned long long* const (&dst)[N]) {
+    if (blockDim.x & 31u) {
+        for (int k = 0; k < N; ++k)
+            if (v[k]) atomicAdd(dst[k], v[k]);
+        return;
+    }
+    __shared__ unsigned long long sh[N];
+    __syncthreads();   // an earlier call in the same kernel may still read sh
+    if (threadIdx.x < (unsigned)N) sh[threadIdx.x] = 0ull;
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < N; ++k) {
+        unsigned long long x = v[k];
+#pragma unroll
+        for (int d = 16; d > 0; d >>= 1) x += __shfl_down_sync(0xffffffffu, x, d);
+        if ((threadIdx.x & 31u) == 0u && x) atomicAdd(&sh[k], x);
+    }
+    __syncthreads();
+    if (threadIdx.x < (unsigned)N && sh[threadIdx.x]) atomicAdd(dst[threadIdx.x], sh[threadIdx.x]);
+}
 constexpr int kDefaultBlock = 256;
+constexpr int kCappedBlocks = 5;   // resident blocks the register-capped batch kernels are built for
 
 }  // namespace pbm
 

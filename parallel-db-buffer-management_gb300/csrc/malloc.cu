@@ -71,11 +71,8 @@ __device__ __forceinline__ void malloc_round(const MArgs& a, uint32_t seed, bool
 }
 
 __device__ __forceinline__ void flush_macc(const MAcc& c, DevStats* st) {
-    if (c.ok) atomicAdd(&st->successes, c.ok);
-    if (c.fail) atomicAdd(&st->failures, c.fail);
-    if (c.steps) atomicAdd(&st->steps, c.steps);
-    if (c.frees) atomicAdd(&st->frees, c.frees);
-    if (c.bad) atomicAdd(&st->bad_frees, c.bad);
+    block_add_counters<5>({c.ok, c.fail, c.steps, c.frees, c.bad},
+                          {&st->successes, &st->failures, &st->steps, &st->frees, &st->bad_frees});
 }
 
 template <bool SERIAL>

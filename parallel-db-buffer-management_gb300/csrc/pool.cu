@@ -56,6 +56,17 @@ __global__ void k_reset_words(uint32_t* words, uint32_t n_words, uint64_t n_page
     }
 }
 
+// Sets the padding bits (pages >= n_pages) of the last words again, e.g.
+// after a caller wrote the bitmap: the walks rely on them never being free.
+__global__ void k_set_padding(uint32_t* words, uint32_t n_words, uint64_t n_pages) {
+    const uint32_t w = (uint32_t)(n_pages >> 5) + threadIdx.x;
+    if (w >= n_words) return;
+    const uint64_t p0 = (uint64_t)w * 32u;
+    uint32_t pad = 0;
+    for (uint32_t b = 0; b < 32; ++b) if (p0 + b >= n_pages) pad |= 1u << b;
+    if (pad) words[w] |= pad;
+}
+
 __device__ __forceinline__ unsigned long long warp_sum64(unsigned long long v) {
 #pragma unroll
     for (int d = 16; d > 0; d >>= 1) v += __shfl_down_sync(0xffffffffu, v, d);
@@ -376,6 +387,8 @@ int pbm_pool_write_bitmap(pbm_pool* pool, const void* h_src, size_t bytes, void*
     if (!pool || !h_src || bytes != pool->bitmap_bytes) return PBM_ERR_INVALID;
     cudaStream_t s = (cudaStream_t)stream;
     PBM_CUDA_TRY(cudaMemcpyAsync(pool->d_words, h_src, bytes, cudaMemcpyHostToDevice, s));
+    k_set_padding<<<1, 64, 0, s>>>(pool->d_words, (uint32_t)(bytes / 4u), pool->n_pages);
+    PBM_LAUNCH_CHECK();
     PBM_CUDA_TRY(cudaStreamSynchronize(s));
     pool->fifo_valid = false;
     return PBM_OK;

@@ -148,6 +148,10 @@ SIGNATURES = [
                                c_void_p]),
     ("pbm_alloc_runs_serial", c_int, [c_void_p, c_uint32, c_void_p, c_uint32, c_uint32, c_void_p,
                                       c_void_p, c_void_p]),
+    ("pbm_alloc_spans", c_int, [c_void_p, c_uint32, c_void_p, c_uint32, c_uint32, c_void_p, c_void_p,
+                                c_void_p]),
+    ("pbm_alloc_spans_serial", c_int, [c_void_p, c_uint32, c_void_p, c_uint32, c_uint32, c_void_p,
+                                       c_void_p, c_void_p]),
     ("pbm_free_runs", c_int, [c_void_p, c_uint32, c_void_p, c_void_p, c_void_p]),
     ("pbm_claim_write_free", c_int, [c_void_p, c_uint32, c_uint32, c_uint32, c_int, c_uint32, c_void_p,
                                      c_void_p, c_void_p]),
@@ -236,7 +240,7 @@ def _check(fn, rc, allow=()):
 
 
 def walk_config(strategy=COLLAB_RW_BM, word_bits=32, collab_width=32, stride=1, max_steps=4096,
-                block_size=256, blocks_per_sm=0, free_merge=1) -> WalkConfig:
+                block_size=256, blocks_per_sm=0, free_merge=0) -> WalkConfig:
     return WalkConfig(strategy, word_bits, collab_width, stride, max_steps, block_size, blocks_per_sm,
                       free_merge)
 
@@ -327,6 +331,12 @@ class Pool:
         fn = self.lib.pbm_alloc_runs_serial if serial else self.lib.pbm_alloc_runs
         return _check("pbm_alloc_runs", fn(self.h, n, _ptr(npages), seed, max_steps, _ptr(ids),
                                            _ptr(steps), stream))
+
+    def alloc_spans(self, n, npages, seed, ids, steps=None, max_steps=4096, stream=0, serial=False):
+        """Runs that may cross word boundaries (1 .. 65536 pages each)."""
+        fn = self.lib.pbm_alloc_spans_serial if serial else self.lib.pbm_alloc_spans
+        return _check("pbm_alloc_spans", fn(self.h, n, _ptr(npages), seed, max_steps, _ptr(ids),
+                                            _ptr(steps), stream))
 
     def free_runs(self, n, ids, npages, stream=0):
         return _check("pbm_free_runs", self.lib.pbm_free_runs(self.h, n, _ptr(ids), _ptr(npages), stream))

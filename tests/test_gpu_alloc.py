@@ -255,6 +255,51 @@ def test_runs_serial_and_parallel(cuda, pbm_mod, orc):
     pool.close()
 
 
+def test_spans_serial_and_parallel(cuda, pbm_mod, orc):
+    """Runs that cross word boundaries: a one-thread replay equals the
+    oracle (ids, steps, bitmap); in parallel, runs of 1..200 pages are
+    disjoint, inside the pool and on free pages, and freeing restores the
+    prefill."""
+    torch = cuda
+    pbm = pbm_mod
+    T, occ = 1 << 15, 0.005
+    pool = _pool(pbm, T, occ, 12)
+    words = orc.bernoulli_bitmap(T, occ, 12)
+    rng = np.random.default_rng(8)
+    k = rng.integers(1, 100, size=120).astype(np.int32)
+    dk = torch.from_numpy(k).cuda()
+    ids = torch.full((120,), -9, dtype=torch.int32, device="cuda")
+    st = torch.zeros(120, dtype=torch.int32, device="cuda")
+    pool.alloc_spans(120, dk, 19, ids, st, serial=True)
+    exp_ids, exp_st = orc.replay_spans(words, T, k, 19)
+    assert np.array_equal(ids.cpu().numpy(), exp_ids)
+    assert np.array_equal(st.cpu().numpy(), exp_st)
+    assert np.array_equal(pool.read_bitmap(), words)
+    assert ((exp_ids[exp_ids >= 0] // 32) != ((exp_ids[exp_ids >= 0] + k[exp_ids >= 0] - 1) // 32)).any()
+    pool.free_runs(120, ids, dk)
+    assert np.array_equal(pool.read_bitmap(), orc.bernoulli_bitmap(T, occ, 12))
+    pool.close()
+    # parallel, on an empty pool of 2^20 pages: 4000 runs of 1..200 pages
+    T = 1 << 20
+    pool = _pool(pbm, T, 0.0, 1)
+    n = 4000
+    k = rng.integers(1, 201, size=n).astype(np.int32)
+    dk = torch.from_numpy(k).cuda()
+    ids = torch.full((n,), -9, dtype=torch.int32, device="cuda")
+    pool.alloc_spans(n, dk, 20, ids, max_steps=1 << 12)
+    h = ids.cpu().numpy()
+    ok = h >= 0
+    assert ok.mean() > 0.99
+    cover = np.zeros(T, dtype=np.int32)
+    for i, kk in zip(h[ok], k[ok]):
+        cover[i:i + kk] += 1
+    assert cover.max() == 1 and (h[ok] + k[ok] <= T).all()
+    assert pool.used() == int(k[ok].sum())
+    pool.free_runs(n, ids, dk)
+    assert pool.used() == 0
+    pool.close()
+
+
 def test_fifo_serial_order(cuda, pbm_mod, orc):
     """Linked-list strategy: FIFO order over the free pages (getPageLinkedList
     pops the head, freePageLinkedList appends at the tail)."""

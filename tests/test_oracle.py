@@ -83,6 +83,60 @@ def test_checker_catches_planted_duplicate(orc):
     assert c.n_duplicates == 1 and c.n_not_marked == 1
 
 
+def test_span_walk_finds_runs_across_words(orc):
+    """Known answers: the only free run of 40 pages starts at page 60 (bits
+    28..31 of word 1, all of word 2, bits 0..3 of word 3) and is found only
+    from a jump to word 1; a 6-page run is found from word 1 (page 60, across
+    words 1/2), word 2 (page 64, inside it) or word 4 (page 157, across 4/5)."""
+    T = 32 * 8
+    w = np.full(8, 0xFFFFFFFF, dtype=np.uint32)
+    w[1] = 0x0FFFFFFF          # pages 60..63 free
+    w[2] = 0                   # pages 64..95 free
+    w[3] = 0xFFFFFFF0          # pages 96..99 free
+    w[4] = 0x1FFFFFFF          # pages 157..159 free
+    w[5] = 0xFFFFFFF8          # pages 160..162 free
+    before = w.copy()
+    L = orc.lib()
+    st = orc.c_int32()
+    found = set()
+    for seed in range(40):
+        x = w.copy()
+        found.add(L.orc_walk_span(orc.P(x), T, 40, seed, 256, orc.ctypes.byref(st)))
+    assert found == {60}
+    found6 = {L.orc_walk_span(orc.P(w.copy()), T, 6, seed, 256, orc.ctypes.byref(st)) for seed in range(40)}
+    assert found6 <= {60, 64, 157} and len(found6) >= 2
+    x = w.copy()
+    assert L.orc_walk_span(orc.P(x), T, 40, 3, 64, orc.ctypes.byref(st)) == 60
+    assert x[2] == 0xFFFFFFFF and x[1] == 0xFFFFFFFF and x[3] == 0xFFFFFFFF
+    L.orc_free_run(orc.P(x), 60, 40)
+    assert np.array_equal(x, before)
+    # no run of 41 pages exists: bounded failure
+    assert L.orc_walk_span(orc.P(w.copy()), T, 41, 1, 64, orc.ctypes.byref(st)) == -1 and st.value == 64
+
+
+def test_span_replay_bitmap_accounting(orc):
+    # an i.i.d. prefill leaves long free stretches only when it is sparse
+    # (P(100 free in a row) = 0.995^100 = 0.6 here)
+    T = 1 << 14
+    w = orc.bernoulli_bitmap(T, 0.005, 5)
+    before = w.copy()
+    k = np.random.default_rng(2).integers(1, 100, size=60)
+    ids, steps = orc.replay_spans(w, T, k, 7)
+    ok = ids >= 0
+    assert ok.mean() > 0.9 and (steps[ok] >= 1).all()
+    cover = np.zeros(T, dtype=np.int32)
+    for i, kk in zip(ids[ok], k[ok]):
+        cover[i:i + kk] += 1
+    assert cover.max() == 1
+    held = np.unpackbits(before.view(np.uint8), bitorder="little")[:T]
+    assert int((held.astype(np.int32) * cover).sum()) == 0
+    assert orc.used_pages(w, T) == orc.used_pages(before, T) + int(k[ok].sum())
+    assert ((ids[ok] // 32) != ((ids[ok] + k[ok] - 1) // 32)).any()     # some runs cross words
+    for i, kk in zip(ids[ok], k[ok]):
+        orc.lib().orc_free_run(orc.P(w), int(i), int(kk))
+    assert np.array_equal(w, before)
+
+
 def test_runs_and_fifo(orc):
     T = 1 << 12
     w = orc.bernoulli_bitmap(T, 0.2, 2)

@@ -55,9 +55,11 @@ MAX_GROUP = 65536
 SEED0 = 1000
 METRIC = "alloc+free ops/s at 90% occupancy (batched persistent kernel, CUDA-graph replay)"
 UNIT = "ops/s"
-# DRAM bytes per alloc+free pair of the batch kernel, from the ncu capture
-# summarised in profiles/batch_persistent_collab32_90pct.md (None until captured).
-NCU_DRAM_BYTES_PER_PAIR = None
+# DRAM bytes per alloc+free pair of the batch kernel: dram__bytes_read.sum +
+# dram__bytes_write.sum of one captured launch (7.81 MB for the 1,420,753-pair
+# step of `bench.py --profile`), summarised in
+# profiles/batch_persistent_collab32_90pct.md.
+NCU_DRAM_BYTES_PER_PAIR = 7.810304e6 / 1420753
 
 
 def env_rank():
@@ -65,6 +67,37 @@ def env_rank():
     w = int(os.environ.get("WORLD_SIZE", "1"))
     lr = int(os.environ.get("LOCAL_RANK", str(r)))
     return r, w, lr
+
+
+WALKS = ("collab32c", "collab32", "collab64c", "word32", "word64", "page")
+
+
+def named_walk(pbm, name):
+    """Walk configurations by name (`--walk`); the `c` forms are the
+    register-capped kernels at 5 blocks per SM, all with unmerged frees."""
+    return {"collab32c": pbm.walk_config(pbm.COLLAB_RW_BM, word_bits=32, collab_width=32, blocks_per_sm=5),
+            "collab32": pbm.walk_config(pbm.COLLAB_RW_BM, word_bits=32, collab_width=32),
+            "collab64c": pbm.walk_config(pbm.COLLAB_RW_BM, word_bits=64, collab_width=32, blocks_per_sm=5),
+            "word32": pbm.walk_config(pbm.RANDOM_WALK_BM, word_bits=32),
+            "word64": pbm.walk_config(pbm.RANDOM_WALK_BM, word_bits=64),
+            "page": pbm.walk_config(pbm.RANDOM_WALK)}[name]
+
+
+def combine_ranks(ms, ops, world, dist=None, device="cpu"):
+    """Whole-job throughput of N independent replicas: every rank ran `ops`
+    operations in `ms` milliseconds of device time; the job's time is the
+    slowest rank's (max over ranks), its work the sum.  Returns (max_ms, ops/s)."""
+    if dist is not None and world > 1:
+        import torch
+
+        t = torch.tensor([float(ms), float(ops)], dtype=torch.float64, device=device)
+        mx = t[:1].clone()
+        dist.all_reduce(mx, op=dist.ReduceOp.MAX)
+        dist.all_reduce(t[1:], op=dist.ReduceOp.SUM)
+        ms, total = float(mx.item()), float(t[1].item())
+    else:
+        total = float(ops) * world
+    return ms, total / (ms * 1e-3)
 
 
 def group_counts(n_steps, seed=GROUP_SEED):
@@ -267,10 +300,12 @@ def run_ours(args, rank, world, local_rank):
     d_tab = torch.from_numpy(tab.view(np.uint8).reshape(-1).copy()).to(dev)
     flush = torch.empty(512 << 20, dtype=torch.uint8, device=dev)
     # autotuner (untimed): candidates run on step 0's groups, swaps keep the pool at 90%
-    tuned = pool.autotune(d_tab[:N_GROUPS * 16], N_GROUPS, int(counts[0].sum()), arena, H, seed=SEED0 - 999,
-                          reps=4, stream=sh)
-    torch.cuda.synchronize()
-    cfg = pbm.walk_config(pbm.COLLAB_RW_BM, word_bits=32, collab_width=32, blocks_per_sm=5)
+    tuned = []
+    if args.walk == "auto":
+        tuned = pool.autotune(d_tab[:N_GROUPS * 16], N_GROUPS, int(counts[0].sum()), arena, H, seed=SEED0 - 999,
+                              reps=4, stream=sh)
+        torch.cuda.synchronize()
+    cfg = named_walk(pbm, "collab32c" if args.walk == "auto" else args.walk)
     if tuned:
         cfg = pbm.WalkConfig.from_buffer_copy(tuned[0].cfg)
 
@@ -318,11 +353,7 @@ def run_ours(args, rank, world, local_rank):
     pairs_per_step = counts.sum(axis=1)
     g_ms = sum(ms for _, ms in res_graph)
     g_ops = sum(2 * int(pairs_per_step[s]) for s, _ in res_graph)
-    if dist:
-        t = torch.tensor([g_ms], device=dev, dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        g_ms = float(t.item())
-    value = g_ops * world / (g_ms * 1e-3)
+    g_ms, value = combine_ranks(g_ms, g_ops, world, dist, dev)
     st = pool.stats(sh)
 
     # ---- plain: one launch per group ----
@@ -365,7 +396,7 @@ def run_ours(args, rank, world, local_rank):
     torch.cuda.synchronize()
     res_e2e = timed(e2e_step, range(args.warmup, min(n_steps, args.warmup + 100)))
     e_ms = sum(ms for _, ms in res_e2e)
-    e2e_value = sum(2 * int(pairs_per_step[s]) for s, _ in res_e2e) / (e_ms * 1e-3) * world
+    _, e2e_value = combine_ranks(e_ms, sum(2 * int(pairs_per_step[s]) for s, _ in res_e2e), world, dist, dev)
 
     # ---- invariants after all forms: occupancy unchanged, arena unique ----
     chk = pool.check(arena, H)
@@ -747,6 +778,95 @@ def run_configs(args, torch, pbm, stream):
     return out
 
 
+def run_profile_kernel(args):
+    """Small, bounded cases of the other kernels for ncu captures (a few GB
+    on the device at most, inputs larger than L2 where the kernel reads
+    any): `bufmgr` 16 rounds of 2^18 Zipf fetches on 2^22 frames (k_round),
+    `malloc` 8 rounds of 32 malloc groups + frees on a 2 GiB pool
+    (k_malloc_persistent), `alloc` 2^22 collaborative claims at 50%
+    (k_alloc_collab) followed by `free` of half of them (k_free_pages)."""
+    import torch
+
+    import pbm
+    import workloads
+
+    torch.cuda.set_device(0)
+    sh = torch.cuda.current_stream().cuda_stream
+    flush = torch.empty(512 << 20, dtype=torch.uint8, device="cuda")
+    out = {"profile_kernel": args.profile_kernel}
+    if args.profile_kernel == "bufmgr":
+        R, rounds = 1 << 18, 16
+        pages = workloads.zipf_pages(1 << 24, 0.99, R * rounds, 3)
+        ptr, idx = workloads.release_lists(rounds, R, 0.25, 3)
+        d_pages = torch.from_numpy(pages).cuda()
+        d_idx = torch.from_numpy(idx).cuda()
+        d_frames = torch.full((R * rounds,), -1, dtype=torch.int32, device="cuda")
+        bm = pbm.BufferManager(1 << 24, 1 << 22, policy=pbm.BM_SINGLE_CLOCK)
+        for r in range(rounds):
+            a, b = int(ptr[r]), int(ptr[r + 1])
+            flush.zero_()
+            bm.round(d_frames, d_idx[a:] if b > a else None, b - a, d_pages[r * R:], R, r * R, d_frames[r * R:],
+                     stream=sh)
+        torch.cuda.synchronize()
+        c = bm.counters(sh)
+        out.update(hits=c.hits, misses=c.misses, mismatches=bm.check(sh).mismatches)
+        bm.close()
+    elif args.profile_kernel == "malloc":
+        T, groups, rounds = 1 << 19, 32, 8
+        pool = pbm.Pool(T, PAGE_SIZE, materialize=True)
+        pool.malloc_init()
+        rng = np.random.default_rng(4)
+        counts = np.clip(np.floor(np.exp(rng.uniform(0, math.log(MAX_GROUP + 1), (rounds, groups)))), 1,
+                         MAX_GROUP).astype(np.int64)
+        n_max = int(counts.sum(axis=1).max())
+        sizes = torch.zeros(2 * n_max, dtype=torch.int32, device="cuda")
+        ptrs = torch.zeros(2 * n_max, dtype=torch.int64, device="cuda")
+        dt = np.dtype([("op", "<i4"), ("count", "<u4"), ("offset", "<u8")])
+        prev_c = np.zeros(groups, dtype=np.int64)
+        for r in range(rounds):
+            # this round's mallocs go to slots [0, n); the previous round's blocks,
+            # moved to [n_max, n_max + n_prev), are freed in the same launch
+            c = counts[r]
+            n = int(c.sum())
+            sizes[:n].copy_(torch.from_numpy(np.clip(np.exp(rng.uniform(math.log(16), math.log(65536), n)), 16,
+                                                     65536).astype(np.int32)))
+            tab = np.zeros(2 * groups, dtype=dt)
+            tab["op"][:groups], tab["count"][:groups] = pbm.OP_MALLOC, c
+            tab["offset"][:groups] = np.concatenate([[0], np.cumsum(c)[:-1]])
+            tab["op"][groups:], tab["count"][groups:] = pbm.OP_MFREE, prev_c
+            tab["offset"][groups:] = n_max + np.concatenate([[0], np.cumsum(prev_c)[:-1]])
+            d_tab = torch.from_numpy(tab.view(np.uint8).copy()).cuda()
+            flush.zero_()
+            pool.malloc_batch(d_tab, None, 2 * groups, sizes, ptrs, 2 * n_max, 77 + r, pbm.LAUNCH_PERSISTENT,
+                              max_steps=512, stream=sh)
+            ptrs[n_max:].zero_()
+            ptrs[n_max:n_max + n].copy_(ptrs[:n])
+            ptrs[:n_max].zero_()
+            prev_c = c
+        torch.cuda.synchronize()
+        st = pool.stats(sh)
+        out.update(successes=st.successes, failures=st.failures, frees=st.frees)
+        pool.close()
+    else:
+        pool = pbm.Pool(T_PAGES, PAGE_SIZE)
+        pool.prefill(0.5, PREFILL_SEED, sh)
+        N = 1 << 22
+        ids = torch.empty(N, dtype=torch.int32, device="cuda")
+        cfg = pbm.walk_config(pbm.COLLAB_RW_BM)
+        for r in range(3):
+            flush.zero_()
+            pool.alloc(cfg, N, 50 + r, ids, stream=sh)
+            sel = ids[: N // 2].contiguous()
+            flush.zero_()
+            pool.free(cfg, sel.numel(), sel, stream=sh)
+        torch.cuda.synchronize()
+        st = pool.stats(sh)
+        out.update(successes=st.successes, failures=st.failures, frees=st.frees, used=pool.used(sh))
+        pool.close()
+    print(json.dumps(out))
+    return 0
+
+
 def run_profile_case(args):
     """The batched form only, for ncu: the same pool, occupancy and groups as
     the benchmark, without page memory (the kernel never touches it), L2
@@ -810,6 +930,10 @@ def main():
     ap.add_argument("--profile-walk", default="collab32c", choices=["collab32c", "collab32", "collab64", "word32"],
                     help="collab32c: collaborative walk, 32-bit words, register-capped 5 blocks/SM, "
                          "frees unmerged (the autotuner's pick at 90%%)")
+    ap.add_argument("--walk", default="auto", choices=("auto",) + WALKS,
+                    help="auto: the autotuner picks (untimed, before the timed steps); else a fixed walk")
+    ap.add_argument("--profile-kernel", default=None, choices=["bufmgr", "malloc", "alloc"],
+                    help="a small case of another kernel, for ncu (alloc also runs the free kernel)")
     ap.add_argument("--configs", default="all",
                     help="other workloads measured after the headline: all, none, or a comma list of "
                          "claim_write_free_50pct,occupancy_sweep,buffer_manager,malloc,serving")
@@ -817,6 +941,8 @@ def main():
     rank, world, local_rank = env_rank()
     if args.profile:
         return run_profile_case(args)
+    if args.profile_kernel:
+        return run_profile_kernel(args)
     if args.impl == "reference":
         return run_reference(args, rank)
     return run_ours(args, rank, world, local_rank)

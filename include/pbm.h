@@ -384,6 +384,25 @@ int pbm_server_run(pbm_server *s, const pbm_request *h_reqs, uint64_t n, pbm_req
 int pbm_server_tenant_pages(pbm_server *s, uint32_t tenant, int32_t *h_out, uint64_t max_out, uint64_t *h_n);
 int pbm_server_destroy(pbm_server *s);
 
+/* ---------------- monitor: occupancy sampled while kernels run ----------------
+ * [monitorBufferRandomWalk, parallelPage.cu:209-223, as a host-polled
+ * sampler]  A host thread samples the pool every interval_us on its own
+ * non-blocking stream (a popcount kernel over the bitmap and a copy of the
+ * statistics block) until max_samples or pbm_monitor_stop; its kernel fits
+ * beside the pool's persistent kernels, so samples are taken while they run.
+ * The pool must outlive the monitor. */
+typedef struct {
+    double   t_s;            /* seconds since pbm_monitor_start */
+    uint64_t used_pages;
+    double   free_fraction;
+    pbm_stats stats;         /* the pool's counters at that time */
+} pbm_monitor_sample;
+typedef struct pbm_monitor pbm_monitor;
+int pbm_monitor_start(pbm_pool *pool, uint32_t interval_us, uint32_t max_samples, pbm_monitor **out);
+/* Copies up to max_out samples taken so far; *h_n = samples taken. */
+int pbm_monitor_samples(pbm_monitor *m, pbm_monitor_sample *h_out, uint32_t max_out, uint32_t *h_n);
+int pbm_monitor_stop(pbm_monitor *m);
+
 /* ---------------- checks and measurement ---------------- */
 
 /* Invariants of an allocation result: ids in range, no page handed to two

@@ -140,15 +140,21 @@ __device__ __forceinline__ uint32_t find_group_warp(const unsigned long long* pr
 // The persistent batch kernel.  With a.fuse each block scans the step's
 // group counts into shared memory itself (no separate prefix kernel); with
 // a.done the last block to finish advances the graph's step counter (no
-// separate step kernel), so one graph replay is one launch.  (Prefetching the
-// next chunk's arena slots and bitmap line into L2 was measured slower: the
-// extra instructions cost more than the latency they hid.)
+// separate step kernel), so one graph replay is one launch.  A warp serves
+// 32 requests (a chunk) at a time.  Each block owns a contiguous range of the
+// step's chunks and its warps take the next one from a shared-memory counter,
+// so a warp whose chunks needed extra jumps does not hold the block's end
+// back (static striding left the slowest of ~8 chunks per warp as the tail).
+// (Prefetching the next chunk's arena slots and bitmap line into L2 was
+// measured slower: the extra instructions cost more than the latency they hid.)
 template <BWalk K, int W, typename Word, int MINB>
 __global__ void __launch_bounds__(256, MINB) k_batch_persistent(BatchArgs a) {
     extern __shared__ unsigned long long s_prefix[];
     __shared__ int32_t slots[256];
     __shared__ bool s_last;
+    __shared__ unsigned int s_next_chunk;
     BAcc acc;
+    if (threadIdx.x == 0) s_next_chunk = 0u;
     const uint32_t step = a.d_step ? *a.d_step : 0u;
     const pbm_group* groups = a.groups + (a.d_step ? (size_t)(step % a.n_steps) * a.n_groups : 0);
     const uint32_t seed = a.seed + step;
@@ -156,6 +162,8 @@ __global__ void __launch_bounds__(256, MINB) k_batch_persistent(BatchArgs a) {
     if (a.fuse) {
         block_exclusive_prefix(groups, a.n_groups, s_prefix);
         pre = s_prefix;
+    } else {
+        __syncthreads();
     }
     const unsigned long long total = pre[a.n_groups];
     const uint32_t lane = threadIdx.x & 31u;
@@ -163,17 +171,22 @@ __global__ void __launch_bounds__(256, MINB) k_batch_persistent(BatchArgs a) {
     const uint32_t L = WordTraits<Word>::count(a.v);
     const uint32_t lane_off = (uint32_t)(((unsigned long long)gl * a.stride) % L);
     volatile int32_t* gslots = slots + (threadIdx.x & ~(uint32_t)(W - 1));
-    const unsigned long long warp0 = ((unsigned long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const unsigned long long nwarps = ((unsigned long long)gridDim.x * blockDim.x) >> 5;
-    uint32_t g_next = 0xffffffffu;     // group of the warp's next chunk
-    for (unsigned long long chunk = warp0; chunk * 32ull < total; chunk += nwarps) {
+    const unsigned long long n_chunks = (total + 31ull) >> 5;
+    const unsigned long long per_block = (n_chunks + gridDim.x - 1ull) / gridDim.x;
+    const unsigned long long c_begin = (unsigned long long)blockIdx.x * per_block;
+    const unsigned long long c_end = min(n_chunks, c_begin + per_block);
+    uint32_t g_lo = 0;                 // group of the warp's previous chunk (chunks only grow)
+    for (;;) {
+        uint32_t k = 0;
+        if (lane == 0) k = atomicAdd(&s_next_chunk, 1u);
+        k = __shfl_sync(0xffffffffu, k, 0);
+        const unsigned long long chunk = c_begin + k;
+        if (chunk >= c_end) break;
         const unsigned long long q0 = chunk * 32ull;
         const unsigned long long q = q0 + lane;
         const bool active = q < total;
-        // group of the chunk's first request, found by the whole warp while it
-        // handled the previous chunk (chunks of a warp are nwarps*32 apart)
-        const uint32_t g0 = g_next != 0xffffffffu ? g_next : find_group_warp(pre, a.n_groups, q0, 0u);
-        if (q0 + nwarps * 32ull < total) g_next = find_group_warp(pre, a.n_groups, q0 + nwarps * 32ull, g0);
+        const uint32_t g0 = find_group_warp(pre, a.n_groups, q0, g_lo);
+        g_lo = g0;
         const unsigned long long g0_end = pre[g0 + 1u];
         int op = PBM_OP_ALLOC;
         unsigned long long slot = 0;

@@ -121,6 +121,10 @@ class ServerConfig(Structure):
                 ("max_occupancy", c_double), ("drain_timeout_s", c_double), ("walk", WalkConfig)]
 
 
+class MonitorSample(Structure):
+    _fields_ = [("t_s", c_double), ("used_pages", c_uint64), ("free_fraction", c_double), ("stats", Stats)]
+
+
 class ServerReport(Structure):
     _fields_ = [("requests", c_uint64), ("completed", c_uint64), ("rejected", c_uint64), ("pages", c_uint64),
                 ("batches", c_uint64), ("max_in_flight", c_uint64), ("wall_s", c_double), ("p50_s", c_double),
@@ -192,6 +196,9 @@ SIGNATURES = [
     ("pbm_server_run", c_int, [c_void_p, POINTER(Request), c_uint64, POINTER(RequestResult), POINTER(ServerReport)]),
     ("pbm_server_tenant_pages", c_int, [c_void_p, c_uint32, c_void_p, c_uint64, POINTER(c_uint64)]),
     ("pbm_server_destroy", c_int, [c_void_p]),
+    ("pbm_monitor_start", c_int, [c_void_p, c_uint32, c_uint32, POINTER(c_void_p)]),
+    ("pbm_monitor_samples", c_int, [c_void_p, POINTER(MonitorSample), c_uint32, POINTER(c_uint32)]),
+    ("pbm_monitor_stop", c_int, [c_void_p]),
     ("pbm_version", c_char_p, []),
     ("pbm_kernel_launches", c_uint64, []),
     ("pbm_device_sm_count", c_int, [POINTER(c_int)]),
@@ -521,6 +528,35 @@ class Server:
     def __del__(self):
         try:
             self.close()
+        except Exception:
+            pass
+
+
+class Monitor:
+    """Occupancy and counters of a pool, sampled on a host thread while kernels run."""
+
+    def __init__(self, pool: Pool, interval_us=100, max_samples=100000):
+        self.lib = lib()
+        h = c_void_p()
+        _check("pbm_monitor_start", self.lib.pbm_monitor_start(pool.h, interval_us, max_samples, byref(h)))
+        self.h = h
+        self.max_samples = max_samples
+
+    def samples(self):
+        out = (MonitorSample * self.max_samples)()
+        n = c_uint32()
+        _check("pbm_monitor_samples", self.lib.pbm_monitor_samples(self.h, out, self.max_samples, byref(n)))
+        return [out[i] for i in range(min(n.value, self.max_samples))]
+
+    def stop(self):
+        if self.h:
+            rc = self.lib.pbm_monitor_stop(self.h)
+            self.h = None
+            _check("pbm_monitor_stop", rc)
+
+    def __del__(self):
+        try:
+            self.stop()
         except Exception:
             pass
 

@@ -656,9 +656,13 @@ def config_malloc(torch, pbm, stream, flush, rounds=16, plain_rounds=4, max_step
            "ops": "mallocs + frees", "l2": "flushed before every round", "max_steps": max_steps,
            "note": "the trace outgrows the pool (about 34 GB live before each round's frees on 32 GiB), "
                    "so part of every round fails after max_steps jumps"}
-    for form in ("graph", "plain"):
+    for form in ("graph", "plain", "queue_graph"):
+        queue = form == "queue_graph"
         pool = pbm.Pool(T, PAGE_SIZE, materialize=True)
-        pool.malloc_init()
+        if queue:
+            pool.qmalloc_init(1 << 22)
+        else:
+            pool.malloc_init()
         gen.manual_seed(4)
         slots = n_max + live_cap
         ptrs = torch.zeros(slots, dtype=torch.int64, device="cuda")
@@ -666,11 +670,12 @@ def config_malloc(torch, pbm, stream, flush, rounds=16, plain_rounds=4, max_step
         n_groups = 2 * N_GROUPS
         dt = np.dtype([("op", "<i4"), ("count", "<u4"), ("offset", "<u8")])
         d_tab = torch.zeros(n_groups * 16, dtype=torch.uint8, device="cuda")
-        graph = (pool.malloc_graph(d_tab, n_groups, 1, sizes, ptrs, slots, 91, max_steps=max_steps, stream=sh)
-                 if form == "graph" else None)
+        mk_graph = pool.qmalloc_graph if queue else pool.malloc_graph
+        graph = (mk_graph(d_tab, n_groups, 1, sizes, ptrs, slots, 91, max_steps=max_steps, stream=sh)
+                 if form != "plain" else None)
         live = torch.empty(0, dtype=torch.int64, device="cuda")
         t_ms, ops, fails = 0.0, 0, 0
-        nr = rounds if form == "graph" else plain_rounds
+        nr = plain_rounds if form == "plain" else rounds
         for r in range(nr):
             c = counts[r]
             n_new = int(c.sum())
@@ -706,13 +711,21 @@ def config_malloc(torch, pbm, stream, flush, rounds=16, plain_rounds=4, max_step
             if live.numel() > live_cap:
                 live = live[:live_cap]
             ops += n_new + k
-        lv, bad = pool.malloc_counts(sh)
         out[form] = {"value": ops / (t_ms * 1e-3), "ms_total": t_ms, "rounds": nr, "failures": fails,
-                     "live_blocks": int(lv), "bad_frees": int(bad), "used_pages": pool.used(sh)}
+                     "used_pages": pool.used(sh)}
+        if queue:
+            queued, chunks, overflow, timeouts, bad = pool.qmalloc_counts(sh)
+            out[form].update(queued_blocks=int(sum(queued)), chunks=int(chunks), overflow=int(overflow),
+                             timeouts=int(timeouts), bad_frees=int(bad))
+        else:
+            lv, bad = pool.malloc_counts(sh)
+            out[form].update(live_blocks=int(lv), bad_frees=int(bad))
         if graph is not None:
             graph.close()
         pool.close()
     out["graph_over_plain"] = out["graph"]["value"] / out["plain"]["value"]
+    out["backends"] = {"graph, plain": "page runs with live counts per run (pbm_malloc_*)",
+                       "queue_graph": "per-class block queues (pbm_qmalloc_*), CUDA-graph form"}
     return out
 
 

@@ -251,6 +251,33 @@ int pbm_malloc_graph_create(pbm_pool *pool, const pbm_group *d_groups, uint32_t 
  * double frees); synchronous. */
 int pbm_malloc_counts(pbm_pool *pool, uint64_t *h_live_runs, uint64_t *h_bad_frees, void *stream);
 
+/* ---------------- queue-based size classes (no reference counterpart) ----------------
+ * The same malloc / free batches over a second backend: per size class a
+ * bounded FIFO ring of free blocks, as the page queues of the allocator the
+ * reference vendors as its comparator (Ouroboros,
+ * source/Ouroboros/include/device/queues/page/PageQueueVL_impl.cuh).  Lanes of
+ * a warp that ask for one class take blocks with one reservation; lanes the
+ * ring cannot serve carve chunks (one page for classes below a page, one block
+ * above) from the pool with the spanning walk and enqueue the blocks nobody
+ * took; frees go back to their class's ring.  Chunks stay with their class
+ * until release.  ring_capacity: blocks per class ring (power of two,
+ * 0 = 2^20); a free into a full ring drops the block (counted).  Pools up to
+ * 64 GiB (32-bit handles of 16 bytes); needs PBM_POOL_MATERIALIZE.  Frees are
+ * not checked for doubles. */
+int pbm_qmalloc_init(pbm_pool *pool, uint32_t ring_capacity);
+int pbm_qmalloc_release(pbm_pool *pool);
+int pbm_qmalloc_batch(pbm_pool *pool, const pbm_group *d_groups, const pbm_group *h_groups, uint32_t n_groups,
+                      const uint32_t *d_sizes, unsigned long long *d_ptrs, uint64_t arena_len, uint32_t seed,
+                      uint32_t max_steps, int mode, void *stream);
+int pbm_qmalloc_graph_create(pbm_pool *pool, const pbm_group *d_groups, uint32_t n_groups, uint32_t n_steps,
+                             const uint32_t *d_sizes, unsigned long long *d_ptrs, uint64_t arena_len,
+                             uint32_t seed0, uint32_t max_steps, void *stream, pbm_graph **out);
+/* h_queued[13]: blocks waiting in each class ring (16 B .. 64 KiB); chunks
+ * carved so far; blocks dropped by full rings; bounded waits that gave up;
+ * frees rejected (outside the pool, not at a block start, no chunk). */
+int pbm_qmalloc_counts(pbm_pool *pool, uint64_t *h_queued, uint64_t *h_chunks, uint64_t *h_overflow,
+                       uint64_t *h_timeouts, uint64_t *h_bad_frees, void *stream);
+
 /* Autotuner (no reference counterpart).  Runs the caller's batch of
  * `requests` swap requests (descriptors in d_groups, all PBM_OP_SWAP) through
  * the persistent kernel for every candidate configuration -- walk, width

@@ -306,3 +306,50 @@ class MallocReplay:
 
     def free(self, offset):
         return self.L.orc_malloc_free(ctypes.byref(self.m), int(offset))
+
+
+class QMallocT(Structure):
+    _fields_ = [("words", c_void_p), ("n_pages", c_uint32), ("page_shift", c_uint32), ("cap", c_uint32),
+                ("class_of", c_void_p), ("ring", c_void_p), ("head", c_uint64 * 13), ("tail", c_uint64 * 13),
+                ("avail", c_int64 * 13), ("space", c_int64 * 13), ("chunks", c_uint64), ("overflow", c_uint64),
+                ("bad_frees", c_uint64)]
+
+
+class QMallocReplay:
+    """Sequential replay of the queue-based size classes (oracle_qmalloc.c)
+    on a bitmap the caller owns (mutated in place)."""
+
+    def __init__(self, words, n_pages, page_shift, cap=1 << 12):
+        L = lib()
+        L.orc_qmalloc_init.argtypes = [ctypes.POINTER(QMallocT), _P, c_uint32, c_uint32, c_uint32]
+        L.orc_qmalloc_init.restype = c_int
+        L.orc_qmalloc_destroy.argtypes = [ctypes.POINTER(QMallocT)]
+        L.orc_qmalloc_group.argtypes = [ctypes.POINTER(QMallocT), _P, c_int, _P, c_uint32, _P, _P]
+        L.orc_qmalloc_free_group.argtypes = [ctypes.POINTER(QMallocT), _P, c_int, _P]
+        self.L = L
+        self.words = words
+        self.q = QMallocT()
+        if L.orc_qmalloc_init(ctypes.byref(self.q), P(words), n_pages, page_shift, cap) != 0:
+            raise MemoryError("orc_qmalloc_init")
+
+    def group(self, sizes, seed_own, max_steps=4096):
+        sizes = np.ascontiguousarray(sizes, dtype=np.uint64)
+        seed_own = np.ascontiguousarray(seed_own, dtype=np.int32)
+        offs = np.zeros(len(sizes), dtype=np.int64)
+        steps = np.zeros(len(sizes), dtype=np.int32)
+        self.L.orc_qmalloc_group(ctypes.byref(self.q), P(sizes), len(sizes), P(seed_own), max_steps, P(offs),
+                                 P(steps))
+        return offs, steps
+
+    def free(self, offsets):
+        offsets = np.ascontiguousarray(offsets, dtype=np.int64)
+        ok = np.zeros(len(offsets), dtype=np.int32)
+        self.L.orc_qmalloc_free_group(ctypes.byref(self.q), P(offsets), len(offsets), P(ok))
+        return ok
+
+    def queued(self):
+        return [int(self.q.avail[c]) for c in range(13)]
+
+    def close(self):
+        if self.q.ring:
+            self.L.orc_qmalloc_destroy(ctypes.byref(self.q))

@@ -245,6 +245,24 @@ void orc_malloc_group(orc_malloc_t *m, const uint64_t *sizes, int lanes, int32_t
 /* 1 = freed, 0 = rejected (outside the pool or no live block). */
 int orc_malloc_free(orc_malloc_t *m, int64_t offset);
 
+/* Queue-based size classes (oracle_qmalloc.c). */
+typedef struct {
+    uint32_t *words;
+    uint32_t n_pages;
+    uint32_t page_shift;
+    uint32_t cap;            /* slots per class ring (power of two) */
+    uint8_t *class_of;       /* per page: class + 1 (| 0x80 past a chunk's first page) */
+    uint32_t *ring;          /* 13 * cap handles (0xffffffff = empty) */
+    uint64_t head[13], tail[13];
+    int64_t avail[13], space[13];
+    uint64_t chunks, overflow, bad_frees;
+} orc_qmalloc_t;
+int orc_qmalloc_init(orc_qmalloc_t *q, uint32_t *words, uint32_t n_pages, uint32_t page_shift, uint32_t cap);
+void orc_qmalloc_destroy(orc_qmalloc_t *q);
+void orc_qmalloc_group(orc_qmalloc_t *q, const uint64_t *sizes, int lanes, const int32_t *seed_own,
+                       uint32_t max_steps, int64_t *offsets, int32_t *steps);
+void orc_qmalloc_free_group(orc_qmalloc_t *q, const int64_t *offsets, int lanes, int32_t *ok);
+
 /* ------------------------------------------------------------------ */
 /* std::atomic host replay (CPU baseline), cpu_replay.cpp              */
 /* ------------------------------------------------------------------ */

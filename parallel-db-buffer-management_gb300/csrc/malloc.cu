@@ -1,6 +1,8 @@
-// malloc.cu -- batched size-classed malloc / free (pbm/pbm_malloc.cuh) over a
-// pool's pages: plain (one launch per group), persistent (one launch), a
-// one-warp deterministic replay, and the CUDA-graph form.
+// malloc.cu -- batched size-classed malloc / free over a pool's pages, with
+// two backends: page runs with live counts (pbm/pbm_malloc.cuh) and per-class
+// block queues (pbm/pbm_qmalloc.cuh).  Forms: plain (one launch per group),
+// persistent (one launch), a one-warp deterministic replay, and the
+// CUDA-graph form.
 //
 // Reference: mallocRW / freeRW (source/RWMalloc.cuh:299-334), the
 // KernelMallocCollab allocator (source/malloc.cu:223-320) and the
@@ -9,12 +11,14 @@
 
 #include "batch_common.cuh"
 #include "pbm/pbm_malloc.cuh"
+#include "pbm/pbm_qmalloc.cuh"
 
 namespace pbm {
 namespace {
 
 struct MArgs {
     MallocView m;
+    QMallocView qm;
     const pbm_group* groups;
     uint32_t n_groups;
     const uint32_t* d_step;
@@ -41,7 +45,8 @@ __device__ __forceinline__ unsigned long long wrap(unsigned long long slot, unsi
     return slot;
 }
 
-template <bool SERIAL>
+// Q: the queue backend (pbm_qmalloc.cuh), else page runs (pbm_malloc.cuh).
+template <bool SERIAL, bool Q>
 __device__ __forceinline__ void malloc_round(const MArgs& a, uint32_t seed, bool active, int op,
                                              unsigned long long q0, unsigned long long q,
                                              unsigned long long slot, MAcc& acc) {
@@ -49,8 +54,13 @@ __device__ __forceinline__ void malloc_round(const MArgs& a, uint32_t seed, bool
     const bool do_free = active && op == PBM_OP_MFREE;
     const uint64_t size = do_malloc ? (uint64_t)a.sizes[slot] : 0ull;
     int32_t s = 0;
-    void* p = malloc_group(a.m, 0xffffffffu, size, request_seed(seed ^ 0x9E3779B9u, (uint32_t)q0),
-                           request_seed(seed, (uint32_t)q), a.max_steps, SERIAL, &s);
+    void* p;
+    if constexpr (Q) {
+        p = qmalloc_group(a.qm, 0xffffffffu, size, request_seed(seed, (uint32_t)q), a.max_steps, SERIAL, &s);
+    } else {
+        p = malloc_group(a.m, 0xffffffffu, size, request_seed(seed ^ 0x9E3779B9u, (uint32_t)q0),
+                         request_seed(seed, (uint32_t)q), a.max_steps, SERIAL, &s);
+    }
     if (do_malloc) {
         a.ptrs[slot] = (unsigned long long)p;
         if (size) {
@@ -60,7 +70,9 @@ __device__ __forceinline__ void malloc_round(const MArgs& a, uint32_t seed, bool
         }
     }
     const void* fp = do_free ? (const void*)a.ptrs[slot] : nullptr;
-    const bool ok = free_group(a.m, 0xffffffffu, fp);
+    bool ok;
+    if constexpr (Q) ok = qfree_group(a.qm, 0xffffffffu, fp);
+    else ok = free_group(a.m, 0xffffffffu, fp);
     if (do_free) {
         a.ptrs[slot] = 0ull;
         if (fp) {
@@ -75,7 +87,7 @@ __device__ __forceinline__ void flush_macc(const MAcc& c, DevStats* st) {
                           {&st->successes, &st->failures, &st->steps, &st->frees, &st->bad_frees});
 }
 
-template <bool SERIAL>
+template <bool SERIAL, bool Q>
 __global__ void __launch_bounds__(256) k_malloc_persistent(MArgs a) {
     MAcc acc;
     const uint32_t step = a.d_step ? *a.d_step : 0u;
@@ -101,11 +113,12 @@ __global__ void __launch_bounds__(256) k_malloc_persistent(MArgs a) {
             op = gd.op;
             slot = wrap(gd.offset + (q - __ldg(a.prefix + g)), a.arena_len);
         }
-        malloc_round<SERIAL>(a, seed, active, op, q0, q, slot, acc);
+        malloc_round<SERIAL, Q>(a, seed, active, op, q0, q, slot, acc);
     }
     flush_macc(acc, a.stats);
 }
 
+template <bool Q>
 __global__ void __launch_bounds__(256) k_malloc_plain(MArgs a) {
     MAcc acc;
     const uint32_t lane = threadIdx.x & 31u;
@@ -114,7 +127,7 @@ __global__ void __launch_bounds__(256) k_malloc_plain(MArgs a) {
     for (unsigned long long chunk = warp0; chunk * 32ull < a.count; chunk += nwarps) {
         const unsigned long long ql = chunk * 32ull + lane;
         const bool active = ql < a.count;
-        malloc_round<false>(a, a.seed, active, a.op, a.q_base + chunk * 32ull, a.q_base + ql,
+        malloc_round<false, Q>(a, a.seed, active, a.op, a.q_base + chunk * 32ull, a.q_base + ql,
                             wrap(a.offset + ql, a.arena_len), acc);
     }
     flush_macc(acc, a.stats);
@@ -129,12 +142,28 @@ __global__ void k_malloc_init(int32_t* start_of, int32_t* live, uint8_t* len_of,
 }
 
 struct MallocTables {
+    // page-run backend
     int32_t* start_of = nullptr;
     int32_t* live = nullptr;
     uint8_t* len_of = nullptr;
+    // queue backend
+    QueueRing* rings = nullptr;
+    uint32_t* slots = nullptr;
+    uint8_t* class_of = nullptr;
+    unsigned long long* qcounters = nullptr;
+    uint32_t qcap = 0;
+    // shared
     unsigned long long* prefix = nullptr;
     uint32_t prefix_cap = 0;
 };
+
+__global__ void k_qmalloc_init(QueueRing* rings, uint32_t capacity) {
+    const int c = threadIdx.x;
+    if (c < kQClasses) {
+        rings[c].head = rings[c].tail = rings[c].avail = 0ull;
+        rings[c].space = capacity;
+    }
+}
 
 }  // namespace
 }  // namespace pbm
@@ -156,16 +185,40 @@ MallocTables* tables_of(pbm_pool* p) {
     return nullptr;
 }
 
+MallocTables* tables_add(pbm_pool* p) {
+    if (MallocTables* t = tables_of(p)) return t;
+    if (g_nreg >= 64) return nullptr;
+    g_reg[g_nreg].pool = p;
+    g_reg[g_nreg].t = MallocTables{};
+    return &g_reg[g_nreg++].t;
+}
+
+uint32_t page_shift_of(const pbm_pool* p) {
+    uint32_t sh = 0;
+    while ((1u << sh) < p->page_size) ++sh;
+    return sh;
+}
+
 MallocView view_of(pbm_pool* p, const MallocTables* t) {
     MallocView m;
     m.pool = p->view;
     m.start_of = t->start_of;
     m.live = t->live;
     m.len_of = t->len_of;
-    uint32_t sh = 0;
-    while ((1u << sh) < p->page_size) ++sh;
-    m.page_shift = sh;
+    m.page_shift = page_shift_of(p);
     return m;
+}
+
+QMallocView qview_of(pbm_pool* p, const MallocTables* t) {
+    QMallocView q;
+    q.pool = p->view;
+    q.rings = t->rings;
+    q.slots = t->slots;
+    q.class_of = t->class_of;
+    q.counters = t->qcounters;
+    q.capacity = t->qcap;
+    q.page_shift = page_shift_of(p);
+    return q;
 }
 
 int check_pool(pbm_pool* p) {
@@ -175,66 +228,61 @@ int check_pool(pbm_pool* p) {
     return PBM_OK;
 }
 
-}  // namespace
-
-extern "C" {
-
-int pbm_malloc_init(pbm_pool* pool) {
-    int rc = check_pool(pool);
-    if (rc) return rc;
-    if (tables_of(pool)) return PBM_OK;
-    if (g_nreg >= 64) return PBM_ERR_NOMEM;
-    MallocTables t;
-    const size_t n = pool->n_pages;
-    if (cudaMalloc(&t.start_of, n * 4) != cudaSuccess || cudaMalloc(&t.live, n * 4) != cudaSuccess ||
-        cudaMalloc(&t.len_of, n) != cudaSuccess) {
-        cudaGetLastError();
-        cudaFree(t.start_of);
-        cudaFree(t.live);
-        return PBM_ERR_NOMEM;
-    }
-    k_malloc_init<<<sm_count() * 4, 256>>>(t.start_of, t.live, t.len_of, (uint32_t)n);
-    PBM_LAUNCH_CHECK();
-    PBM_CUDA_TRY(cudaDeviceSynchronize());
-    g_reg[g_nreg].pool = pool;
-    g_reg[g_nreg].t = t;
-    ++g_nreg;
-    return PBM_OK;
+void free_queue(MallocTables* t) {
+    cudaFree(t->rings);
+    cudaFree(t->slots);
+    cudaFree(t->class_of);
+    cudaFree(t->qcounters);
+    t->rings = nullptr;
+    t->slots = nullptr;
+    t->class_of = nullptr;
+    t->qcounters = nullptr;
+    t->qcap = 0;
 }
 
-int pbm_malloc_tables(pbm_pool* pool, void** d_start_of, void** d_live, void** d_len_of) {
-    MallocTables* t = tables_of(pool);
-    if (!t) return PBM_ERR_INVALID;
-    if (d_start_of) *d_start_of = t->start_of;
-    if (d_live) *d_live = t->live;
-    if (d_len_of) *d_len_of = t->len_of;
-    return PBM_OK;
-}
-
-int pbm_malloc_release(pbm_pool* pool) {
+void drop_if_empty(pbm_pool* p) {
     for (int i = 0; i < g_nreg; ++i) {
-        if (g_reg[i].pool != pool) continue;
-        cudaDeviceSynchronize();
-        cudaFree(g_reg[i].t.start_of);
-        cudaFree(g_reg[i].t.live);
-        cudaFree(g_reg[i].t.len_of);
-        cudaFree(g_reg[i].t.prefix);
-        g_reg[i] = g_reg[--g_nreg];
-        return PBM_OK;
+        if (g_reg[i].pool != p) continue;
+        MallocTables& t = g_reg[i].t;
+        if (!t.start_of && !t.rings) {
+            cudaFree(t.prefix);
+            g_reg[i] = g_reg[--g_nreg];
+        }
+        return;
     }
-    return PBM_ERR_INVALID;
 }
 
-int pbm_malloc_batch(pbm_pool* pool, const pbm_group* d_groups, const pbm_group* h_groups, uint32_t n_groups,
-                     const uint32_t* d_sizes, unsigned long long* d_ptrs, uint64_t arena_len, uint32_t seed,
-                     uint32_t max_steps, int mode, void* stream) {
+bool ensure_prefix(MallocTables* t, uint32_t n_groups) {
+    if (t->prefix_cap >= n_groups + 1u) return true;
+    cudaFree(t->prefix);
+    t->prefix = nullptr;
+    if (cudaMalloc(&t->prefix, sizeof(unsigned long long) * (n_groups + 1u)) != cudaSuccess) {
+        cudaGetLastError();
+        t->prefix_cap = 0;
+        return false;
+    }
+    t->prefix_cap = n_groups + 1u;
+    return true;
+}
+
+template <bool Q>
+int persistent_blocks() {
+    int per_sm = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_malloc_persistent<false, Q>, 256, 0);
+    return per_sm < 1 ? 1 : per_sm;
+}
+
+int batch_impl(pbm_pool* pool, bool queue, const pbm_group* d_groups, const pbm_group* h_groups, uint32_t n_groups,
+               const uint32_t* d_sizes, unsigned long long* d_ptrs, uint64_t arena_len, uint32_t seed,
+               uint32_t max_steps, int mode, void* stream) {
     MallocTables* t = tables_of(pool);
-    if (!t || !d_ptrs || !arena_len) return PBM_ERR_INVALID;
+    if (!t || (queue ? !t->rings : !t->start_of) || !d_ptrs || !arena_len) return PBM_ERR_INVALID;
     if (n_groups == 0) return PBM_OK;
     cudaStream_t s = (cudaStream_t)stream;
     pool->fifo_valid = false;
     MArgs a{};
-    a.m = view_of(pool, t);
+    if (queue) a.qm = qview_of(pool, t);
+    else a.m = view_of(pool, t);
     a.seed = seed;
     a.sizes = d_sizes;
     a.ptrs = d_ptrs;
@@ -254,48 +302,43 @@ int pbm_malloc_batch(pbm_pool* pool, const pbm_group* d_groups, const pbm_group*
             a.q_base = q;
             const unsigned long long warps = (gd.count + 31ull) / 32ull;
             const unsigned grid = (unsigned)((warps * 32ull + 255ull) / 256ull);
-            k_malloc_plain<<<grid, 256, 0, s>>>(a);
+            if (queue) k_malloc_plain<true><<<grid, 256, 0, s>>>(a);
+            else k_malloc_plain<false><<<grid, 256, 0, s>>>(a);
             PBM_LAUNCH_CHECK();
             q += gd.count;
         }
         return PBM_OK;
     }
     if ((mode != PBM_LAUNCH_PERSISTENT && mode != PBM_LAUNCH_SERIAL) || !d_groups) return PBM_ERR_INVALID;
-    if (t->prefix_cap < n_groups + 1u) {
-        cudaFree(t->prefix);
-        t->prefix = nullptr;
-        if (cudaMalloc(&t->prefix, sizeof(unsigned long long) * (n_groups + 1u)) != cudaSuccess) {
-            cudaGetLastError();
-            t->prefix_cap = 0;
-            return PBM_ERR_NOMEM;
-        }
-        t->prefix_cap = n_groups + 1u;
-    }
+    if (!ensure_prefix(t, n_groups)) return PBM_ERR_NOMEM;
     k_batch_prefix<<<1, 1024, 0, s>>>(d_groups, n_groups, nullptr, 1u, t->prefix);
     PBM_LAUNCH_CHECK();
     a.groups = d_groups;
     a.n_groups = n_groups;
     a.prefix = t->prefix;
     if (mode == PBM_LAUNCH_SERIAL) {
-        k_malloc_persistent<true><<<1, 32, 0, s>>>(a);
+        if (queue) k_malloc_persistent<true, true><<<1, 32, 0, s>>>(a);
+        else k_malloc_persistent<true, false><<<1, 32, 0, s>>>(a);
+    } else if (queue) {
+        k_malloc_persistent<false, true><<<sm_count() * persistent_blocks<true>(), 256, 0, s>>>(a);
     } else {
-        int per_sm = 0;
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_malloc_persistent<false>, 256, 0);
-        if (per_sm < 1) per_sm = 1;
-        k_malloc_persistent<false><<<sm_count() * per_sm, 256, 0, s>>>(a);
+        k_malloc_persistent<false, false><<<sm_count() * persistent_blocks<false>(), 256, 0, s>>>(a);
     }
     PBM_LAUNCH_CHECK();
     return PBM_OK;
 }
 
-int pbm_malloc_graph_create(pbm_pool* pool, const pbm_group* d_groups, uint32_t n_groups, uint32_t n_steps,
-                            const uint32_t* d_sizes, unsigned long long* d_ptrs, uint64_t arena_len,
-                            uint32_t seed0, uint32_t max_steps, void* stream, pbm_graph** out) {
+int graph_impl(pbm_pool* pool, bool queue, const pbm_group* d_groups, uint32_t n_groups, uint32_t n_steps,
+               const uint32_t* d_sizes, unsigned long long* d_ptrs, uint64_t arena_len, uint32_t seed0,
+               uint32_t max_steps, void* stream, pbm_graph** out) {
     MallocTables* t = tables_of(pool);
-    if (!t || !d_groups || !d_ptrs || !out || !n_groups || !n_steps || !arena_len) return PBM_ERR_INVALID;
+    if (!t || (queue ? !t->rings : !t->start_of) || !d_groups || !d_ptrs || !out || !n_groups || !n_steps ||
+        !arena_len)
+        return PBM_ERR_INVALID;
     *out = nullptr;
     cudaStream_t s = (cudaStream_t)stream;
-    pbm_graph* g = new pbm_graph();
+    pbm_graph* g = new (std::nothrow) pbm_graph();
+    if (!g) return PBM_ERR_NOMEM;
     g->graph = nullptr;
     g->exec = nullptr;
     if (cudaMalloc(&g->d_step, sizeof(uint32_t)) != cudaSuccess ||
@@ -308,7 +351,8 @@ int pbm_malloc_graph_create(pbm_pool* pool, const pbm_group* d_groups, uint32_t 
     PBM_CUDA_TRY(cudaMemsetAsync(g->d_step, 0, sizeof(uint32_t), s));
     PBM_CUDA_TRY(cudaStreamSynchronize(s));
     MArgs a{};
-    a.m = view_of(pool, t);
+    if (queue) a.qm = qview_of(pool, t);
+    else a.m = view_of(pool, t);
     a.groups = d_groups;
     a.n_groups = n_groups;
     a.d_step = g->d_step;
@@ -320,15 +364,14 @@ int pbm_malloc_graph_create(pbm_pool* pool, const pbm_group* d_groups, uint32_t 
     a.prefix = g->d_prefix;
     a.max_steps = max_steps ? max_steps : kDefaultMaxSteps;
     a.stats = pool->d_stats;
-    int per_sm = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_malloc_persistent<false>, 256, 0);
-    if (per_sm < 1) per_sm = 1;
+    const int per_sm = queue ? persistent_blocks<true>() : persistent_blocks<false>();
     cudaStream_t cap = nullptr;
     PBM_CUDA_TRY(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
     cudaError_t e = cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal);
     if (e == cudaSuccess) {
         k_batch_prefix<<<1, 1024, 0, cap>>>(d_groups, n_groups, g->d_step, n_steps, g->d_prefix);
-        k_malloc_persistent<false><<<sm_count() * per_sm, 256, 0, cap>>>(a);
+        if (queue) k_malloc_persistent<false, true><<<sm_count() * per_sm, 256, 0, cap>>>(a);
+        else k_malloc_persistent<false, false><<<sm_count() * per_sm, 256, 0, cap>>>(a);
         k_step_advance<<<1, 32, 0, cap>>>(g->d_step);
         cudaGraph_t graph = nullptr;
         e = cudaStreamEndCapture(cap, &graph);
@@ -352,9 +395,75 @@ int pbm_malloc_graph_create(pbm_pool* pool, const pbm_group* d_groups, uint32_t 
     return PBM_OK;
 }
 
-int pbm_malloc_counts(pbm_pool* pool, uint64_t* h_live_runs, uint64_t* h_bad_frees, void* stream) {
+}  // namespace
+
+extern "C" {
+
+int pbm_malloc_init(pbm_pool* pool) {
+    int rc = check_pool(pool);
+    if (rc) return rc;
+    MallocTables* t = tables_add(pool);
+    if (!t) return PBM_ERR_NOMEM;
+    if (t->start_of) return PBM_OK;
+    const size_t n = pool->n_pages;
+    if (cudaMalloc(&t->start_of, n * 4) != cudaSuccess || cudaMalloc(&t->live, n * 4) != cudaSuccess ||
+        cudaMalloc(&t->len_of, n) != cudaSuccess) {
+        cudaGetLastError();
+        cudaFree(t->start_of);
+        cudaFree(t->live);
+        t->start_of = nullptr;
+        t->live = nullptr;
+        t->len_of = nullptr;
+        drop_if_empty(pool);
+        return PBM_ERR_NOMEM;
+    }
+    k_malloc_init<<<sm_count() * 4, 256>>>(t->start_of, t->live, t->len_of, (uint32_t)n);
+    PBM_LAUNCH_CHECK();
+    PBM_CUDA_TRY(cudaDeviceSynchronize());
+    return PBM_OK;
+}
+
+int pbm_malloc_tables(pbm_pool* pool, void** d_start_of, void** d_live, void** d_len_of) {
+    MallocTables* t = tables_of(pool);
+    if (!t || !t->start_of) return PBM_ERR_INVALID;
+    if (d_start_of) *d_start_of = t->start_of;
+    if (d_live) *d_live = t->live;
+    if (d_len_of) *d_len_of = t->len_of;
+    return PBM_OK;
+}
+
+int pbm_malloc_release(pbm_pool* pool) {
     MallocTables* t = tables_of(pool);
     if (!t) return PBM_ERR_INVALID;
+    cudaDeviceSynchronize();
+    cudaFree(t->start_of);
+    cudaFree(t->live);
+    cudaFree(t->len_of);
+    t->start_of = nullptr;
+    t->live = nullptr;
+    t->len_of = nullptr;
+    free_queue(t);
+    drop_if_empty(pool);
+    return PBM_OK;
+}
+
+int pbm_malloc_batch(pbm_pool* pool, const pbm_group* d_groups, const pbm_group* h_groups, uint32_t n_groups,
+                     const uint32_t* d_sizes, unsigned long long* d_ptrs, uint64_t arena_len, uint32_t seed,
+                     uint32_t max_steps, int mode, void* stream) {
+    return batch_impl(pool, false, d_groups, h_groups, n_groups, d_sizes, d_ptrs, arena_len, seed, max_steps, mode,
+                      stream);
+}
+
+int pbm_malloc_graph_create(pbm_pool* pool, const pbm_group* d_groups, uint32_t n_groups, uint32_t n_steps,
+                            const uint32_t* d_sizes, unsigned long long* d_ptrs, uint64_t arena_len,
+                            uint32_t seed0, uint32_t max_steps, void* stream, pbm_graph** out) {
+    return graph_impl(pool, false, d_groups, n_groups, n_steps, d_sizes, d_ptrs, arena_len, seed0, max_steps, stream,
+                      out);
+}
+
+int pbm_malloc_counts(pbm_pool* pool, uint64_t* h_live_runs, uint64_t* h_bad_frees, void* stream) {
+    MallocTables* t = tables_of(pool);
+    if (!t || !t->start_of) return PBM_ERR_INVALID;
     cudaStream_t s = (cudaStream_t)stream;
     DevStats d;
     PBM_CUDA_TRY(cudaMemcpyAsync(&d, pool->d_stats, sizeof(d), cudaMemcpyDeviceToHost, s));
@@ -372,6 +481,79 @@ int pbm_malloc_counts(pbm_pool* pool, uint64_t* h_live_runs, uint64_t* h_bad_fre
         if (e != cudaSuccess) { cudaGetLastError(); return PBM_ERR_CUDA; }
         *h_live_runs = c;
     }
+    return PBM_OK;
+}
+
+// ---- queue backend ----
+
+int pbm_qmalloc_init(pbm_pool* pool, uint32_t ring_capacity) {
+    int rc = check_pool(pool);
+    if (rc) return rc;
+    if (pool->n_pages * (uint64_t)pool->page_size > (1ull << 36)) return PBM_ERR_INVALID;   // 32-bit handles of 16 B
+    const uint32_t cap = ring_capacity ? ring_capacity : (1u << 20);
+    if (cap & (cap - 1u)) return PBM_ERR_INVALID;
+    MallocTables* t = tables_add(pool);
+    if (!t) return PBM_ERR_NOMEM;
+    if (t->rings) return t->qcap == cap ? PBM_OK : PBM_ERR_INVALID;
+    const size_t n = pool->n_pages;
+    if (cudaMalloc(&t->rings, sizeof(QueueRing) * kQClasses) != cudaSuccess ||
+        cudaMalloc(&t->slots, sizeof(uint32_t) * (size_t)kQClasses * cap) != cudaSuccess ||
+        cudaMalloc(&t->class_of, n) != cudaSuccess ||
+        cudaMalloc(&t->qcounters, sizeof(unsigned long long) * 4) != cudaSuccess) {
+        cudaGetLastError();
+        free_queue(t);
+        drop_if_empty(pool);
+        return PBM_ERR_NOMEM;
+    }
+    t->qcap = cap;
+    PBM_CUDA_TRY(cudaMemset(t->slots, 0xff, sizeof(uint32_t) * (size_t)kQClasses * cap));
+    PBM_CUDA_TRY(cudaMemset(t->class_of, 0, n));
+    PBM_CUDA_TRY(cudaMemset(t->qcounters, 0, sizeof(unsigned long long) * 4));
+    k_qmalloc_init<<<1, 32>>>(t->rings, cap);
+    PBM_LAUNCH_CHECK();
+    PBM_CUDA_TRY(cudaDeviceSynchronize());
+    return PBM_OK;
+}
+
+int pbm_qmalloc_release(pbm_pool* pool) {
+    MallocTables* t = tables_of(pool);
+    if (!t || !t->rings) return PBM_ERR_INVALID;
+    cudaDeviceSynchronize();
+    free_queue(t);
+    drop_if_empty(pool);
+    return PBM_OK;
+}
+
+int pbm_qmalloc_batch(pbm_pool* pool, const pbm_group* d_groups, const pbm_group* h_groups, uint32_t n_groups,
+                      const uint32_t* d_sizes, unsigned long long* d_ptrs, uint64_t arena_len, uint32_t seed,
+                      uint32_t max_steps, int mode, void* stream) {
+    return batch_impl(pool, true, d_groups, h_groups, n_groups, d_sizes, d_ptrs, arena_len, seed, max_steps, mode,
+                      stream);
+}
+
+int pbm_qmalloc_graph_create(pbm_pool* pool, const pbm_group* d_groups, uint32_t n_groups, uint32_t n_steps,
+                             const uint32_t* d_sizes, unsigned long long* d_ptrs, uint64_t arena_len,
+                             uint32_t seed0, uint32_t max_steps, void* stream, pbm_graph** out) {
+    return graph_impl(pool, true, d_groups, n_groups, n_steps, d_sizes, d_ptrs, arena_len, seed0, max_steps, stream,
+                      out);
+}
+
+int pbm_qmalloc_counts(pbm_pool* pool, uint64_t* h_queued, uint64_t* h_chunks, uint64_t* h_overflow,
+                       uint64_t* h_timeouts, uint64_t* h_bad_frees, void* stream) {
+    MallocTables* t = tables_of(pool);
+    if (!t || !t->rings) return PBM_ERR_INVALID;
+    cudaStream_t s = (cudaStream_t)stream;
+    QueueRing r[kQClasses];
+    unsigned long long c[4];
+    PBM_CUDA_TRY(cudaMemcpyAsync(r, t->rings, sizeof(r), cudaMemcpyDeviceToHost, s));
+    PBM_CUDA_TRY(cudaMemcpyAsync(c, t->qcounters, sizeof(c), cudaMemcpyDeviceToHost, s));
+    PBM_CUDA_TRY(cudaStreamSynchronize(s));
+    if (h_queued)
+        for (int k = 0; k < kQClasses; ++k) h_queued[k] = (uint64_t)(long long)r[k].avail;
+    if (h_chunks) *h_chunks = c[kQChunks];
+    if (h_overflow) *h_overflow = c[kQOverflow];
+    if (h_timeouts) *h_timeouts = c[kQTimeouts];
+    if (h_bad_frees) *h_bad_frees = c[kQBadFrees];
     return PBM_OK;
 }
 

@@ -180,6 +180,14 @@ SIGNATURES = [
     ("pbm_malloc_graph_create", c_int, [c_void_p, c_void_p, c_uint32, c_uint32, c_void_p, c_void_p, c_uint64,
                                         c_uint32, c_uint32, c_void_p, POINTER(c_void_p)]),
     ("pbm_malloc_counts", c_int, [c_void_p, POINTER(c_uint64), POINTER(c_uint64), c_void_p]),
+    ("pbm_qmalloc_init", c_int, [c_void_p, c_uint32]),
+    ("pbm_qmalloc_release", c_int, [c_void_p]),
+    ("pbm_qmalloc_batch", c_int, [c_void_p, c_void_p, POINTER(Group), c_uint32, c_void_p, c_void_p, c_uint64,
+                                  c_uint32, c_uint32, c_int, c_void_p]),
+    ("pbm_qmalloc_graph_create", c_int, [c_void_p, c_void_p, c_uint32, c_uint32, c_void_p, c_void_p, c_uint64,
+                                         c_uint32, c_uint32, c_void_p, POINTER(c_void_p)]),
+    ("pbm_qmalloc_counts", c_int, [c_void_p, POINTER(c_uint64), POINTER(c_uint64), POINTER(c_uint64),
+                                   POINTER(c_uint64), POINTER(c_uint64), c_void_p]),
     ("pbm_autotune", c_int, [c_void_p, c_void_p, c_uint32, c_uint64, c_void_p, c_uint64, c_uint32, c_int,
                              c_uint32, POINTER(TuneResult), c_uint32, POINTER(c_uint32), c_void_p]),
     ("pbm_bufmgr_create", c_int, [POINTER(BufMgrConfig), c_void_p, POINTER(c_void_p)]),
@@ -392,6 +400,34 @@ class Pool:
         live, bad = c_uint64(), c_uint64()
         _check("pbm_malloc_counts", self.lib.pbm_malloc_counts(self.h, byref(live), byref(bad), stream))
         return live.value, bad.value
+
+    # queue-based size classes -------------------------------------------------------
+    def qmalloc_init(self, ring_capacity=0):
+        _check("pbm_qmalloc_init", self.lib.pbm_qmalloc_init(self.h, ring_capacity))
+
+    def qmalloc_release(self):
+        _check("pbm_qmalloc_release", self.lib.pbm_qmalloc_release(self.h))
+
+    def qmalloc_batch(self, d_groups, h_groups, n_groups, sizes, ptrs, arena_len, seed, mode, max_steps=4096,
+                      stream=0):
+        return _check("pbm_qmalloc_batch",
+                      self.lib.pbm_qmalloc_batch(self.h, _ptr(d_groups), h_groups, n_groups, _ptr(sizes), _ptr(ptrs),
+                                                 arena_len, seed, max_steps, mode, stream))
+
+    def qmalloc_graph(self, d_groups, n_groups, n_steps, sizes, ptrs, arena_len, seed0, max_steps=4096, stream=0):
+        g = c_void_p()
+        _check("pbm_qmalloc_graph_create",
+               self.lib.pbm_qmalloc_graph_create(self.h, _ptr(d_groups), n_groups, n_steps, _ptr(sizes),
+                                                 _ptr(ptrs), arena_len, seed0, max_steps, stream, byref(g)))
+        return Graph(self.lib, g)
+
+    def qmalloc_counts(self, stream=0):
+        """(queued per class [13], chunks, overflow, timeouts, bad frees)"""
+        q = (c_uint64 * 13)()
+        ch, ov, to, bf = c_uint64(), c_uint64(), c_uint64(), c_uint64()
+        _check("pbm_qmalloc_counts", self.lib.pbm_qmalloc_counts(self.h, q, byref(ch), byref(ov), byref(to),
+                                                                 byref(bf), stream))
+        return list(q), ch.value, ov.value, to.value, bf.value
 
     def autotune(self, d_groups, n_groups, requests, arena, arena_len, seed=77, reps=3, max_steps=4096,
                  max_out=64, stream=0):

@@ -187,3 +187,43 @@ def test_malloc_replay_blocks_and_release(orc):
         assert rep.free(o) == 1
     assert rep.free(offs[0]) == 0          # double free is rejected
     assert np.array_equal(w, before)
+
+
+def test_qmalloc_replay_reuses_queued_blocks(orc):
+    """Queue backend: blocks are aligned to their class (page-aligned above a
+    page), disjoint and inside the pool; freed blocks come back first (FIFO)
+    before any new chunk is carved; everything freed sits in the queues."""
+    T, shift = 1 << 12, 12
+    w = orc.empty_bitmap(T)
+    q = orc.QMallocReplay(w, T, shift, cap=1 << 12)
+    rng = np.random.default_rng(3)
+    seeds = lambda g: np.array([orc.lib().orc_seed(11, g * 32 + l) for l in range(32)], dtype=np.int32)
+    blocks = []
+    for g in range(8):
+        sizes = np.clip(np.exp(rng.uniform(np.log(16), np.log(65536), 32)), 16, 65536).astype(np.uint64)
+        offs, _ = q.group(sizes, seeds(g))
+        assert (offs >= 0).all()
+        cls = np.maximum(16, 1 << np.ceil(np.log2(sizes.astype(np.float64))).astype(np.int64))
+        assert (offs % np.minimum(cls, 1 << shift) == 0).all()
+        blocks += list(zip(offs.tolist(), cls.tolist()))
+    s = sorted(blocks)
+    assert all(a + la <= b for (a, la), (b, _) in zip(s, s[1:]))
+    assert s[-1][0] + s[-1][1] <= T << shift
+    chunks = q.q.chunks
+    used = orc.used_pages(w, T)
+    offs = np.array([b for b, _ in blocks], dtype=np.int64)
+    for i in range(0, len(offs), 32):
+        assert q.free(offs[i:i + 32]).all()
+    queued = q.queued()
+    pages = sum(n * (1 << (4 + c)) for c, n in enumerate(queued)) >> shift
+    assert pages == used and q.q.overflow == 0          # every carved block is queued again
+    # the same requests again: served from the queues, no new chunk
+    rng = np.random.default_rng(3)
+    for g in range(8):
+        sizes = np.clip(np.exp(rng.uniform(np.log(16), np.log(65536), 32)), 16, 65536).astype(np.uint64)
+        offs2, _ = q.group(sizes, seeds(g))
+        assert (offs2 >= 0).all()
+    assert q.q.chunks == chunks and orc.used_pages(w, T) == used
+    bad = q.free(np.array([8, (T << shift) + 16, -1], dtype=np.int64))
+    assert list(bad) == [0, 0, 1] and q.q.bad_frees == 2
+    q.close()

@@ -407,7 +407,10 @@ def run_ours(args, rank, world, local_rank):
     ceil_line, _ = pbm.atomic_ceiling(words=1 << 22, threads=pbm_sms() * 2048, iters=64, returning=1, pattern=1)
     ceil_spread, _ = pbm.atomic_ceiling(words=1 << 22, threads=pbm_sms() * 2048, iters=64, returning=1,
                                         pattern=2)
-    ceil_ops = max(ceil_line, ceil_spread)
+    # the ceiling: uncontended atomicOr on distinct words spread over L2 slices
+    # (32 lanes on 32 lines), the pattern of the frees and of per-page claims;
+    # the one-line pattern (32 lanes on one 128-byte line) is reported beside it
+    ceil_ops = ceil_spread
     pairs_s = value / 2 / world
     atomic_achieved = 2 * pairs_s          # algorithmic RMWs: one claim + one release per pair
     bytes_per_pair = 16                    # 4 B arena read + 4 B write + 2 x 4 B bitmap RMW
@@ -424,7 +427,9 @@ def run_ours(args, rank, world, local_rank):
     roofline = {
         "bound": "l2_atomic", "achieved": atomic_achieved / 1e9, "peak": ceil_ops / 1e9, "unit": "Gatomic/s",
         "frac": atomic_achieved / ceil_ops, "traffic": traffic,
-        "kernel": "k_batch_persistent<Collab,32,u32> (+ its 1-block prefix and step kernels in the graph)",
+        "peak_source": "pbm_atomic_ceiling, spread pattern (uncontended atomicOr, 32 lanes on 32 lines), same run",
+        "line_pattern_peak": ceil_line / 1e9, "frac_of_line_pattern": atomic_achieved / ceil_line,
+        "kernel": "k_batch_persistent<Collab,32,u32,5>: one launch per graph replay",
         "hbm": {"achieved": hbm_achieved, "peak": hbm_peak, "unit": "GB/s", "frac": hbm_achieved / hbm_peak,
                 "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)" if peaks else "fallback"},
     }
@@ -529,6 +534,7 @@ def config_occupancy_sweep(torch, pbm, stream, flush, rounds=16, N=1 << 22, max_
             pool.reset(sh)
             if occ > 0:
                 pool.prefill(occ, PREFILL_SEED, sh)
+            free0 = T_PAGES - pool.used(sh)          # the realised free pages of the prefill
             gen.manual_seed(PREFILL_SEED)
             t_ms, ops, fails, round0_steps, per_round = 0.0, 0, 0, None, []
             for r in range(rounds):
@@ -545,7 +551,12 @@ def config_occupancy_sweep(torch, pbm, stream, flush, rounds=16, N=1 << 22, max_
                 t_ms += ta + tf
                 ops += N + sel.numel()
                 per_round.append([round(ta, 4), round(tf, 4), int(got.numel())])
+            # RW_TAS(T, A, N) = (T/N) ln(A / (A - N)), the mean probes of N page-probe
+            # requests on A free pages (theoretical_models.py:20-21); reported where A >= 1.25 N
+            # (near A = N the model diverges and failures at max_steps truncate the walk)
+            model = (T_PAGES / N) * math.log(free0 / (free0 - N)) if wname == "page_probe" and free0 >= 1.25 * N else None
             row[wname] = {"value": ops / (t_ms * 1e-3), "ms_total": t_ms, "failures": fails,
+                          "model_rw_tas_round0": model,
                           "round0_ops_s": (N + per_round[0][2] // 2) / ((per_round[0][0] + per_round[0][1]) * 1e-3),
                           "round0_granted": per_round[0][2], "mean_steps_round0": round0_steps,
                           "used_after": pool.used(sh), "per_round_ms_alloc_free_granted": per_round}

@@ -223,9 +223,11 @@ __device__ __forceinline__ int32_t walk_word(const PoolView& v, int32_t seed0,
 // and lowest bits first, one atomicOr per word -- and hands the bits it
 // gained to the needing lanes in lane order (needing lane of rank r takes
 // the r-th gained bit).  Nothing is over-claimed, so nothing is written back.
-// When a concurrent claim took some of the planned bits, the group plans
-// once more in the same words from the values its atomics returned (no new
-// load, no new jump) before it jumps again.  Lanes whose words coincide
+// Needs left unmet (too few free bits, or bits a concurrent claim took
+// first) go to the next jump.  (Planning once more in the same words from the
+// values the atomics returned saved few jumps and cost more instructions
+// than it saved on GB300, so a lost bit simply waits for the next jump.)
+// Lanes whose words coincide
 // (only possible when W*stride > L) are de-duplicated with __match_any_sync.
 //
 // Every lane of the group must call this converged; `need` says whether the
@@ -278,16 +280,13 @@ __device__ __forceinline__ int32_t walk_collab(const PoolView& v, bool need, int
             uint32_t peers = __match_any_sync(gmask, w);
             if ((peers & lt) != 0u) fr = 0;                          // a lower lane reads this word
         }
-        for (int pass = 0;; ++pass) {
+        {
             const int cnt = popc_w(fr);
             const int incl = group_incl_scan<W>(cnt, gl, gmask);
             const int n = __popc(needm);
             const Word m = low_bits(fr, n - (incl - cnt));
-            Word got = 0, old = 0;
-            if (m) {
-                old = atomic_or(words + w, m);
-                got = m & (Word)~old;
-            }
+            Word got = 0;
+            if (m) got = m & (Word)~atomic_or(words + w, m);
             const bool lost = __ballot_sync(gmask, got != m) != 0u;
             const int g = popc_w(got);
             // inclusive prefix of the bits gained, and their total
@@ -324,9 +323,6 @@ __device__ __forceinline__ int32_t walk_collab(const PoolView& v, bool need, int
                     id = (int32_t)((src_w << T::kShift) + nth_bit(src_got, r - src_excl));
             }
             needm = __ballot_sync(gmask, need && id < 0);
-            if (!needm || !lost || pass > 0) break;
-            // plan again in the same words: the atomics returned their state
-            if (m) fr = (Word)~(old | m);
         }
     }
     if (steps_out) *steps_out = (int32_t)s;

@@ -5,12 +5,15 @@
 // run the same requests:
 //   plain       one kernel launch per group (what a caller gets by launching
 //               its own kernel per batch, unitTest1.cu:64 style);
-//   persistent  one kernel over all groups, a grid of (SMs x resident blocks)
-//               warps striding over 32-request chunks; each lane finds its
-//               group by binary search in the groups' prefix sums;
-//   graph       the persistent form captured once in a CUDA graph together
-//               with its prefix kernel and a step-advance kernel, so each
-//               replay reads the next step's descriptors from device memory.
+//   persistent  one kernel over all groups, a grid of (SMs x resident blocks);
+//               each block scans the groups' counts into shared memory and
+//               its warps pull 32-request chunks of the block's range from a
+//               shared counter, finding a chunk's group by a ballot search of
+//               the prefix sums;
+//   graph       the persistent form captured once in a CUDA graph; the last
+//               block to finish advances the device-resident step counter, so
+//               each replay is one launch that reads the next step's
+//               descriptors from device memory.
 #include "batch_common.cuh"
 
 namespace pbm {
@@ -42,35 +45,16 @@ struct BatchArgs {
     unsigned long long q_base;
 };
 
+// Per-thread counters of a launch; ok / fail / frees count requests of the
+// thread (at most one per chunk it serves), steps may pass 2^32.
 struct BAcc {
-    unsigned long long ok = 0, fail = 0, steps = 0, frees = 0;
+    uint32_t ok = 0, fail = 0, frees = 0;
+    unsigned long long steps = 0;
 };
 
 __device__ __forceinline__ void flush_bacc(const BAcc& a, DevStats* st) {
-    __shared__ unsigned long long sh[4];
-    if (threadIdx.x == 0) { sh[0] = sh[1] = sh[2] = sh[3] = 0; }
-    __syncthreads();
-    unsigned long long v0 = a.ok, v1 = a.fail, v2 = a.steps, v3 = a.frees;
-#pragma unroll
-    for (int d = 16; d > 0; d >>= 1) {
-        v0 += __shfl_down_sync(0xffffffffu, v0, d);
-        v1 += __shfl_down_sync(0xffffffffu, v1, d);
-        v2 += __shfl_down_sync(0xffffffffu, v2, d);
-        v3 += __shfl_down_sync(0xffffffffu, v3, d);
-    }
-    if ((threadIdx.x & 31) == 0) {
-        if (v0) atomicAdd(&sh[0], v0);
-        if (v1) atomicAdd(&sh[1], v1);
-        if (v2) atomicAdd(&sh[2], v2);
-        if (v3) atomicAdd(&sh[3], v3);
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        if (sh[0]) atomicAdd(&st->successes, sh[0]);
-        if (sh[1]) atomicAdd(&st->failures, sh[1]);
-        if (sh[2]) atomicAdd(&st->steps, sh[2]);
-        if (sh[3]) atomicAdd(&st->frees, sh[3]);
-    }
+    block_add_counters<4>({a.ok, a.fail, a.steps, a.frees},
+                          {&st->successes, &st->failures, &st->steps, &st->frees});
 }
 
 // One warp-wide round: every lane of the warp calls converged.

@@ -871,6 +871,54 @@ def run_profile_kernel(args):
         st = pool.stats(sh)
         out.update(successes=st.successes, failures=st.failures, frees=st.frees)
         pool.close()
+    elif args.profile_kernel == "misc":
+        # one launch each: page-probe and word-probe walks (2^22 claims at 50%),
+        # runs across words (2^18 runs of 1..64 pages at 5%), config 1's
+        # claim/write/free, the queue malloc (2^18 requests), the atomicOr
+        # ceiling, and one plain batch launch (a 65,536-request swap group)
+        N = 1 << 22
+        ids = torch.empty(N, dtype=torch.int32, device="cuda")
+        pool = pbm.Pool(T_PAGES, PAGE_SIZE)
+        for name, cfg in (("page", pbm.walk_config(pbm.RANDOM_WALK)), ("word", pbm.walk_config(pbm.RANDOM_WALK_BM))):
+            pool.reset(sh)
+            pool.prefill(0.5, PREFILL_SEED, sh)
+            flush.zero_()
+            pool.alloc(cfg, N, 60, ids, stream=sh)
+        pool.reset(sh)
+        pool.prefill(0.05, PREFILL_SEED, sh)
+        R = 1 << 18
+        k = torch.from_numpy(np.random.default_rng(1).integers(1, 65, R).astype(np.int32)).cuda()
+        flush.zero_()
+        pool.alloc_spans(R, k, 61, ids[:R], max_steps=256, stream=sh)
+        pool.close()
+        small = pbm.Pool(1 << 16, 64, materialize=True)
+        small.prefill(0.5, 1, sh)
+        small.claim_write_free(1 << 15, 1, ids[:1 << 15], stream=sh)
+        small.close()
+        qp = pbm.Pool(1 << 19, PAGE_SIZE, materialize=True)
+        qp.qmalloc_init(1 << 18)
+        sizes = torch.from_numpy(np.clip(np.exp(np.random.default_rng(2).uniform(math.log(16), math.log(65536), R)),
+                                         16, 65536).astype(np.int32)).cuda()
+        ptrs = torch.zeros(R, dtype=torch.int64, device="cuda")
+        dt = np.dtype([("op", "<i4"), ("count", "<u4"), ("offset", "<u8")])
+        tab = np.zeros(1, dtype=dt)
+        tab[0] = (pbm.OP_MALLOC, R, 0)
+        flush.zero_()
+        qp.qmalloc_batch(torch.from_numpy(tab.view(np.uint8).copy()).cuda(), None, 1, sizes, ptrs, R, 62,
+                         pbm.LAUNCH_PERSISTENT, stream=sh)
+        qp.close()
+        pbm.atomic_ceiling(words=1 << 22, threads=pbm_sms() * 2048, iters=64, returning=1, pattern=2)
+        pool = pbm.Pool(T_PAGES, PAGE_SIZE)
+        pool.prefill(OCCUPANCY, PREFILL_SEED, sh)
+        words = pool.read_bitmap(sh)
+        held = np.nonzero(np.unpackbits(words.view(np.uint8), bitorder="little")[:T_PAGES])[0].astype(np.int32)
+        arena = torch.from_numpy(held).cuda()
+        flush.zero_()
+        pool.batch(named_walk(pbm, "collab32c"), None, pbm.groups_array([(pbm.OP_SWAP, 65536, 0)]), 1, arena,
+                   len(held), 63, pbm.LAUNCH_PLAIN, stream=sh)
+        torch.cuda.synchronize()
+        out.update(used=pool.used(sh), held=len(held))
+        pool.close()
     else:
         pool = pbm.Pool(T_PAGES, PAGE_SIZE)
         pool.prefill(0.5, PREFILL_SEED, sh)
@@ -956,7 +1004,7 @@ def main():
                          "frees unmerged (the autotuner's pick at 90%%)")
     ap.add_argument("--walk", default="auto", choices=("auto",) + WALKS,
                     help="auto: the autotuner picks (untimed, before the timed steps); else a fixed walk")
-    ap.add_argument("--profile-kernel", default=None, choices=["bufmgr", "malloc", "alloc"],
+    ap.add_argument("--profile-kernel", default=None, choices=["bufmgr", "malloc", "alloc", "misc"],
                     help="a small case of another kernel, for ncu (alloc also runs the free kernel)")
     ap.add_argument("--configs", default="all",
                     help="other workloads measured after the headline: all, none, or a comma list of "

@@ -69,13 +69,15 @@ def env_rank():
     return r, w, lr
 
 
-WALKS = ("collab32c", "collab32", "collab64c", "word32", "word64", "page")
+WALKS = ("collab32c", "pair32c", "collab32", "collab64c", "word32", "word64", "page")
 
 
 def named_walk(pbm, name):
     """Walk configurations by name (`--walk`); the `c` forms are the
-    register-capped kernels at 5 blocks per SM, all with unmerged frees."""
+    register-capped kernels at 5 blocks per SM, all with unmerged frees;
+    `pair32c` serves two requests per lane (64 per warp, collab_width 64)."""
     return {"collab32c": pbm.walk_config(pbm.COLLAB_RW_BM, word_bits=32, collab_width=32, blocks_per_sm=5),
+            "pair32c": pbm.walk_config(pbm.COLLAB_RW_BM, word_bits=32, collab_width=64, blocks_per_sm=5),
             "collab32": pbm.walk_config(pbm.COLLAB_RW_BM, word_bits=32, collab_width=32),
             "collab64c": pbm.walk_config(pbm.COLLAB_RW_BM, word_bits=64, collab_width=32, blocks_per_sm=5),
             "word32": pbm.walk_config(pbm.RANDOM_WALK_BM, word_bits=32),
@@ -964,6 +966,7 @@ def run_profile_case(args):
     flush = torch.empty(512 << 20, dtype=torch.uint8, device=dev)
     walk = {"collab32c": pbm.walk_config(pbm.COLLAB_RW_BM, word_bits=32, collab_width=32, blocks_per_sm=5,
                                          free_merge=0),
+            "pair32c": pbm.walk_config(pbm.COLLAB_RW_BM, word_bits=32, collab_width=64, blocks_per_sm=5),
             "collab32": pbm.walk_config(pbm.COLLAB_RW_BM, word_bits=32, collab_width=32),
             "collab64": pbm.walk_config(pbm.COLLAB_RW_BM, word_bits=64, collab_width=32),
             "word32": pbm.walk_config(pbm.RANDOM_WALK_BM, word_bits=32)}[args.profile_walk]
@@ -999,7 +1002,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--profile", action="store_true", help="batched form only (for ncu)")
-    ap.add_argument("--profile-walk", default="collab32c", choices=["collab32c", "collab32", "collab64", "word32"],
+    ap.add_argument("--profile-walk", default="collab32c", choices=["collab32c", "pair32c", "collab32", "collab64",
+                                                                     "word32"],
                     help="collab32c: collaborative walk, 32-bit words, register-capped 5 blocks/SM, "
                          "frees unmerged (the autotuner's pick at 90%%)")
     ap.add_argument("--walk", default="auto", choices=("auto",) + WALKS,

@@ -71,7 +71,8 @@ typedef struct {
 typedef struct {
     int32_t  strategy;      /* PBM_RANDOM_WALK ... */
     int32_t  word_bits;     /* 32 or 64 (word-probe and collaborative walks) */
-    int32_t  collab_width;  /* 8, 16 or 32 lanes per collaborating group */
+    int32_t  collab_width;  /* 8, 16 or 32 lanes per collaborating group; batches also take 64:
+                               32 lanes serving two requests each */
     uint32_t stride;        /* words between neighbouring lanes of a collaborating group (>=1) */
     uint32_t max_steps;     /* bound on random jumps per request (0 = 4096) */
     int32_t  block_size;    /* threads per block (0 = 256) */

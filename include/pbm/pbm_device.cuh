@@ -330,6 +330,93 @@ __device__ __forceinline__ int32_t walk_collab(const PoolView& v, bool need, int
 }
 
 // ---------------------------------------------------------------------------
+// The collaborative walk for two requests per lane (a warp serving 64
+// requests at a time): the same jump, window, plan and atomics as
+// walk_collab<32, Word>, with the needing requests ranked a-requests first
+// (lane order), then b-requests; request of rank r takes gained bit r.  The
+// jump's fixed costs (window load, scan, claims) are shared by up to 64
+// requests.  The whole warp calls converged.
+// ---------------------------------------------------------------------------
+template <typename Word>
+__device__ __forceinline__ void collab_take(int r, int gincl, int g, uint32_t w, Word got, int32_t& id) {
+    using T = WordTraits<Word>;
+    int src = 0;
+#pragma unroll
+    for (int step = 16; step >= 1; step >>= 1) {
+        const int gv = __shfl_sync(kFull32, gincl, src + step - 1);
+        if (gv <= r) src += step;
+    }
+    const int src_excl = __shfl_sync(kFull32, gincl - g, src);
+    const uint32_t src_w = __shfl_sync(kFull32, w, src);
+    Word src_got;
+    if constexpr (sizeof(Word) == 8) {
+        const uint32_t lo = __shfl_sync(kFull32, (uint32_t)got, src);
+        const uint32_t hi = __shfl_sync(kFull32, (uint32_t)(got >> 32), src);
+        src_got = ((Word)hi << 32) | (Word)lo;
+    } else {
+        src_got = __shfl_sync(kFull32, got, src);
+    }
+    id = (int32_t)((src_w << T::kShift) + nth_bit(src_got, r - src_excl));
+}
+
+template <typename Word>
+__device__ __forceinline__ void walk_collab2(const PoolView& v, bool need_a, bool need_b, int32_t group_seed,
+                                             uint32_t lane_off, bool dedupe, uint32_t max_steps, int32_t& id_a,
+                                             int32_t& id_b, int32_t* steps_out) {
+    using T = WordTraits<Word>;
+    Word* words = reinterpret_cast<Word*>(v.words);
+    const uint32_t L = T::count(v);
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t lt = (1u << lane) - 1u;
+    id_a = -1;
+    id_b = -1;
+    int32_t x = group_seed & 0x7fffffff;
+    uint32_t ma = __ballot_sync(kFull32, need_a), mb = __ballot_sync(kFull32, need_b);
+    uint32_t s = 0;
+    while ((ma | mb) && s < max_steps) {
+        ++s;
+        x = lcg31(x);
+        uint32_t w = idx_hi(x, L) + lane_off;
+        if (w >= L) w -= L;
+        Word fr = (Word)~load_word(words + w);
+        if (dedupe) {
+            const uint32_t peers = __match_any_sync(kFull32, w);
+            if ((peers & lt) != 0u) fr = 0;                          // a lower lane reads this word
+        }
+        const int cnt = popc_w(fr);
+        const int incl = group_incl_scan<32>(cnt, lane, kFull32);
+        const int na = __popc(ma);
+        const int n = na + __popc(mb);
+        const Word m = low_bits(fr, n - (incl - cnt));
+        Word got = 0;
+        if (m) got = m & (Word)~atomic_or(words + w, m);
+        const bool lost = __ballot_sync(kFull32, got != m) != 0u;
+        const int g = popc_w(got);
+        int gincl, G;
+        if (!lost) {
+            gincl = min(incl, n);
+            G = min(__shfl_sync(kFull32, incl, 31), n);
+        } else {
+            gincl = group_incl_scan<32>(g, lane, kFull32);
+            G = __shfl_sync(kFull32, gincl, 31);
+        }
+        if (G > 0) {
+            const bool wa = need_a && id_a < 0, wb = need_b && id_b < 0;
+            const int ra = wa ? __popc(ma & lt) : 0;
+            const int rb = wb ? na + __popc(mb & lt) : 0;
+            int32_t ta = -1, tb = -1;
+            collab_take<Word>(ra, gincl, g, w, got, ta);
+            if (__any_sync(kFull32, wb && rb < G)) collab_take<Word>(rb, gincl, g, w, got, tb);
+            if (wa && ra < G) id_a = ta;
+            if (wb && rb < G) id_b = tb;
+        }
+        ma = __ballot_sync(kFull32, need_a && id_a < 0);
+        mb = __ballot_sync(kFull32, need_b && id_b < 0);
+    }
+    if (steps_out) *steps_out = (int32_t)s;
+}
+
+// ---------------------------------------------------------------------------
 // The collaborative walk over an arbitrary set of converged lanes `active`
 // (the drop-in form: the reference's getPage runs on __activemask(),
 // CollabRW_BM.cuh:119).  Active lane k (k-th set bit of `active`) reads word

@@ -1,7 +1,8 @@
 // autotune.cu -- picks the batch kernel configuration for a pool's occupancy.
 //
 // The sweep covers the walk (per-thread page probe, per-thread word probe,
-// warp-collaborative), the collaboration width (8 / 16 / 32 lanes), 32- vs
+// warp-collaborative), the collaboration width (8 / 16 / 32 lanes, or 64:
+// 32 lanes serving two requests each), 32- vs
 // 64-bit bitmap words, the walk stride between a group's lanes, and blocks
 // per SM (occupancy-limited, or register-capped at kCappedBlocks), and merged
 // frees.  Every candidate runs the caller's own batch of swap requests through
@@ -46,7 +47,7 @@ std::vector<pbm_walk_config> candidates(uint32_t max_steps) {
             out.push_back(c);
         }
         for (int wb : {32, 64})
-            for (int W : {8, 16, 32})
+            for (int W : {8, 16, 32, 64})
                 for (uint32_t stride : {1u, 33u}) {
                     c = base();
                     c.strategy = PBM_COLLAB_RW_BM;

@@ -18,7 +18,11 @@
 
 namespace pbm {
 
-enum class BWalk { Page, Word32, Word64, Collab };
+// Collab2: the collaborative walk with two requests per lane (64 per warp),
+// selected by collab_width 64.
+enum class BWalk { Page, Word32, Word64, Collab, Collab2 };
+
+template <BWalk K> constexpr int kReqPerLane = K == BWalk::Collab2 ? 2 : 1;
 
 struct BatchArgs {
     PoolView v;
@@ -57,25 +61,10 @@ __device__ __forceinline__ void flush_bacc(const BAcc& a, DevStats* st) {
                           {&st->successes, &st->failures, &st->steps, &st->frees});
 }
 
-// One warp-wide round: every lane of the warp calls converged.
-template <BWalk K, int W, typename Word>
-__device__ __forceinline__ void batch_round(const BatchArgs& a, uint32_t seed, bool active, int op,
-                                            unsigned long long q, unsigned long long slot,
-                                            uint32_t lane_off, volatile int32_t* gslots, BAcc& acc) {
-    const bool need = active && (op == PBM_OP_ALLOC || op == PBM_OP_SWAP);
-    // the slot's held page is read before the walk so its latency overlaps it
-    const int32_t held = (active && op != PBM_OP_ALLOC) ? a.arena[slot] : -1;
-    int32_t s = 0, id = -1;
-    if constexpr (K == BWalk::Collab) {
-        const uint32_t gl = threadIdx.x & (uint32_t)(W - 1);
-        id = walk_collab<W, Word>(a.v, need, request_seed(seed, (uint32_t)(q - gl)), lane_off,
-                                  a.dedupe != 0, a.max_steps, gslots, &s);
-    } else if (need) {
-        const int32_t seed0 = request_seed(seed, (uint32_t)q);
-        if constexpr (K == BWalk::Page) id = walk_page(a.v, seed0, a.max_steps, &s);
-        else if constexpr (K == BWalk::Word32) id = walk_word<uint32_t>(a.v, seed0, a.max_steps, &s);
-        else id = walk_word<uint64_t>(a.v, seed0, a.max_steps, &s);
-    }
+// The request's result: arena update, counters, and the free of the page it
+// gave up (merged per word within the warp when asked); converged call.
+__device__ __forceinline__ void batch_finish(const BatchArgs& a, bool active, int op, unsigned long long slot,
+                                             int32_t held, bool need, int32_t id, int32_t s, BAcc& acc) {
     int32_t to_free = -1;
     if (active) {
         if (op == PBM_OP_ALLOC) {
@@ -97,6 +86,44 @@ __device__ __forceinline__ void batch_round(const BatchArgs& a, uint32_t seed, b
     }
     if (a.merge) free_page_warp(a.v, 0xffffffffu, to_free);
     else if (to_free >= 0) free_page(a.v, to_free);
+}
+
+// One warp-wide round: every lane of the warp calls converged.
+template <BWalk K, int W, typename Word>
+__device__ __forceinline__ void batch_round(const BatchArgs& a, uint32_t seed, bool active, int op,
+                                            unsigned long long q, unsigned long long slot,
+                                            uint32_t lane_off, volatile int32_t* gslots, BAcc& acc) {
+    const bool need = active && (op == PBM_OP_ALLOC || op == PBM_OP_SWAP);
+    // the slot's held page is read before the walk so its latency overlaps it
+    const int32_t held = (active && op != PBM_OP_ALLOC) ? a.arena[slot] : -1;
+    int32_t s = 0, id = -1;
+    if constexpr (K == BWalk::Collab) {
+        const uint32_t gl = threadIdx.x & (uint32_t)(W - 1);
+        id = walk_collab<W, Word>(a.v, need, request_seed(seed, (uint32_t)(q - gl)), lane_off,
+                                  a.dedupe != 0, a.max_steps, gslots, &s);
+    } else if (need) {
+        const int32_t seed0 = request_seed(seed, (uint32_t)q);
+        if constexpr (K == BWalk::Page) id = walk_page(a.v, seed0, a.max_steps, &s);
+        else if constexpr (K == BWalk::Word32) id = walk_word<uint32_t>(a.v, seed0, a.max_steps, &s);
+        else id = walk_word<uint64_t>(a.v, seed0, a.max_steps, &s);
+    }
+    batch_finish(a, active, op, slot, held, need, id, s, acc);
+}
+
+// Two requests per lane (a: q0 + lane, b: q0 + 32 + lane), one walk.
+template <typename Word>
+__device__ __forceinline__ void batch_round2(const BatchArgs& a, uint32_t seed, unsigned long long q0,
+                                             bool act_a, int op_a, unsigned long long slot_a, bool act_b, int op_b,
+                                             unsigned long long slot_b, uint32_t lane_off, BAcc& acc) {
+    const bool need_a = act_a && (op_a == PBM_OP_ALLOC || op_a == PBM_OP_SWAP);
+    const bool need_b = act_b && (op_b == PBM_OP_ALLOC || op_b == PBM_OP_SWAP);
+    const int32_t held_a = (act_a && op_a != PBM_OP_ALLOC) ? a.arena[slot_a] : -1;
+    const int32_t held_b = (act_b && op_b != PBM_OP_ALLOC) ? a.arena[slot_b] : -1;
+    int32_t s = 0, id_a = -1, id_b = -1;
+    walk_collab2<Word>(a.v, need_a, need_b, request_seed(seed, (uint32_t)q0), lane_off, a.dedupe != 0,
+                       a.max_steps, id_a, id_b, &s);
+    batch_finish(a, act_a, op_a, slot_a, held_a, need_a, id_a, s, acc);
+    batch_finish(a, act_b, op_b, slot_b, held_b, need_b, id_b, s, acc);
 }
 
 __device__ __forceinline__ unsigned long long wrap_slot(unsigned long long slot, unsigned long long len) {
@@ -155,7 +182,8 @@ __global__ void __launch_bounds__(256, MINB) k_batch_persistent(BatchArgs a) {
     const uint32_t L = WordTraits<Word>::count(a.v);
     const uint32_t lane_off = (uint32_t)(((unsigned long long)gl * a.stride) % L);
     volatile int32_t* gslots = slots + (threadIdx.x & ~(uint32_t)(W - 1));
-    const unsigned long long n_chunks = (total + 31ull) >> 5;
+    constexpr unsigned long long CH = 32ull * kReqPerLane<K>;    // requests per chunk
+    const unsigned long long n_chunks = (total + CH - 1ull) / CH;
     const unsigned long long per_block = (n_chunks + gridDim.x - 1ull) / gridDim.x;
     const unsigned long long c_begin = (unsigned long long)blockIdx.x * per_block;
     const unsigned long long c_end = min(n_chunks, c_begin + per_block);
@@ -166,22 +194,32 @@ __global__ void __launch_bounds__(256, MINB) k_batch_persistent(BatchArgs a) {
         k = __shfl_sync(0xffffffffu, k, 0);
         const unsigned long long chunk = c_begin + k;
         if (chunk >= c_end) break;
-        const unsigned long long q0 = chunk * 32ull;
-        const unsigned long long q = q0 + lane;
-        const bool active = q < total;
+        const unsigned long long q0 = chunk * CH;
         const uint32_t g0 = find_group_warp(pre, a.n_groups, q0, g_lo);
         g_lo = g0;
         const unsigned long long g0_end = pre[g0 + 1u];
-        int op = PBM_OP_ALLOC;
-        unsigned long long slot = 0;
-        if (active) {
-            // a chunk usually lies inside one group; lanes past its end search on
+        // a chunk usually lies inside one group; requests past its end search on
+        auto locate = [&](unsigned long long q, int& op, unsigned long long& slot) {
             const uint32_t g = q < g0_end ? g0 : find_group_any(pre, a.n_groups, q, g0);
             const pbm_group gd = groups[g];
             op = gd.op;
             slot = wrap_slot(gd.offset + (q - pre[g]), a.arena_len);
+        };
+        const unsigned long long q = q0 + lane;
+        const bool active = q < total;
+        int op = PBM_OP_ALLOC;
+        unsigned long long slot = 0;
+        if (active) locate(q, op, slot);
+        if constexpr (K == BWalk::Collab2) {
+            const unsigned long long qb = q + 32ull;
+            const bool act_b = qb < total;
+            int op_b = PBM_OP_ALLOC;
+            unsigned long long slot_b = 0;
+            if (act_b) locate(qb, op_b, slot_b);
+            batch_round2<Word>(a, seed, q0, active, op, slot, act_b, op_b, slot_b, lane_off, acc);
+        } else {
+            batch_round<K, W, Word>(a, seed, active, op, q, slot, lane_off, gslots, acc);
         }
-        batch_round<K, W, Word>(a, seed, active, op, q, slot, lane_off, gslots, acc);
     }
     flush_bacc(acc, a.stats);
     if (a.done) {
@@ -210,12 +248,18 @@ __global__ void __launch_bounds__(256) k_batch_plain(BatchArgs a) {
     volatile int32_t* gslots = slots + (threadIdx.x & ~(uint32_t)(W - 1));
     const unsigned long long warp0 = ((unsigned long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const unsigned long long nwarps = ((unsigned long long)gridDim.x * blockDim.x) >> 5;
-    for (unsigned long long chunk = warp0; chunk * 32ull < a.count; chunk += nwarps) {
-        const unsigned long long ql = chunk * 32ull + lane;
+    constexpr unsigned long long CH = 32ull * kReqPerLane<K>;
+    for (unsigned long long chunk = warp0; chunk * CH < a.count; chunk += nwarps) {
+        const unsigned long long ql = chunk * CH + lane;
         const bool active = ql < a.count;
-        unsigned long long slot = a.offset + ql;
-        if (slot >= a.arena_len) slot = slot - a.arena_len < a.arena_len ? slot - a.arena_len : slot % a.arena_len;
-        batch_round<K, W, Word>(a, a.seed, active, a.op, a.q_base + ql, slot, lane_off, gslots, acc);
+        const unsigned long long slot = wrap_slot(a.offset + ql, a.arena_len);
+        if constexpr (K == BWalk::Collab2) {
+            const bool act_b = ql + 32ull < a.count;
+            batch_round2<Word>(a, a.seed, a.q_base + chunk * CH, active, a.op, slot, act_b, a.op,
+                               wrap_slot(a.offset + ql + 32ull, a.arena_len), lane_off, acc);
+        } else {
+            batch_round<K, W, Word>(a, a.seed, active, a.op, a.q_base + ql, slot, lane_off, gslots, acc);
+        }
     }
     flush_bacc(acc, a.stats);
 }
@@ -263,7 +307,8 @@ int launch_batch_kw(const BatchArgs& a, bool persistent, int block, int blocks_p
             k_batch_persistent<K, W, Word, 1><<<sm_count() * per_sm, block, smem, s>>>(a);
         }
     } else {
-        unsigned long long warps = (a.count + 31ull) / 32ull;
+        const unsigned long long per_warp = 32ull * kReqPerLane<K>;
+        unsigned long long warps = (a.count + per_warp - 1ull) / per_warp;
         unsigned long long grid = (warps * 32ull + (unsigned long long)block - 1ull) / (unsigned long long)block;
         if (grid < 1) grid = 1;
         k_batch_plain<K, W, Word><<<(unsigned)grid, block, 0, s>>>(a);
@@ -284,6 +329,8 @@ int launch_batch(const pbm_walk_config* c, const BatchArgs& a, bool persistent, 
                    : launch_batch_kw<BWalk::Word32, 32, uint32_t>(a, persistent, block, bps, s);
     case PBM_COLLAB_RW_BM: {
         const int W = c->collab_width ? c->collab_width : 32;
+        if (W == 64) return w64 ? launch_batch_kw<BWalk::Collab2, 32, uint64_t>(a, persistent, block, bps, s)
+                                : launch_batch_kw<BWalk::Collab2, 32, uint32_t>(a, persistent, block, bps, s);
         if (W == 8) return w64 ? launch_batch_kw<BWalk::Collab, 8, uint64_t>(a, persistent, block, bps, s)
                                : launch_batch_kw<BWalk::Collab, 8, uint32_t>(a, persistent, block, bps, s);
         if (W == 16) return w64 ? launch_batch_kw<BWalk::Collab, 16, uint64_t>(a, persistent, block, bps, s)
@@ -314,6 +361,7 @@ int resolve_blocks_per_sm(const pbm_walk_config* c) {
         return w64 ? PBM_FITS(BWalk::Word64, 32, uint64_t) : PBM_FITS(BWalk::Word32, 32, uint32_t);
     default: {
         const int W = c->collab_width ? c->collab_width : 32;
+        if (W == 64) return w64 ? PBM_FITS(BWalk::Collab2, 32, uint64_t) : PBM_FITS(BWalk::Collab2, 32, uint32_t);
         if (W == 8) return w64 ? PBM_FITS(BWalk::Collab, 8, uint64_t) : PBM_FITS(BWalk::Collab, 8, uint32_t);
         if (W == 16) return w64 ? PBM_FITS(BWalk::Collab, 16, uint64_t) : PBM_FITS(BWalk::Collab, 16, uint32_t);
         return w64 ? PBM_FITS(BWalk::Collab, 32, uint64_t) : PBM_FITS(BWalk::Collab, 32, uint32_t);
@@ -334,7 +382,8 @@ BatchArgs base_args(pbm_pool* p, const pbm_walk_config* c, int32_t* arena, uint6
     a.stride = c->stride ? c->stride : 1u;
     a.merge = c->free_merge;
     a.stats = p->d_stats;
-    const int W = c->strategy == PBM_COLLAB_RW_BM ? (c->collab_width ? c->collab_width : 32) : 1;
+    const int Wc = c->strategy == PBM_COLLAB_RW_BM ? (c->collab_width ? c->collab_width : 32) : 1;
+    const int W = Wc == 64 ? 32 : Wc;   // lanes reading the window
     const uint32_t L = c->word_bits == 64 ? p->view.n_words64 : p->view.n_words32;
     a.dedupe = ((unsigned long long)(W - 1) * a.stride >= L) ? 1 : 0;
     return a;
@@ -343,7 +392,8 @@ BatchArgs base_args(pbm_pool* p, const pbm_walk_config* c, int32_t* arena, uint6
 int valid_cfg(const pbm_walk_config* c) {
     if (!c) return PBM_ERR_INVALID;
     if (c->word_bits != 0 && c->word_bits != 32 && c->word_bits != 64) return PBM_ERR_INVALID;
-    if (c->collab_width != 0 && c->collab_width != 8 && c->collab_width != 16 && c->collab_width != 32)
+    if (c->collab_width != 0 && c->collab_width != 8 && c->collab_width != 16 && c->collab_width != 32 &&
+        !(c->collab_width == 64 && c->strategy == PBM_COLLAB_RW_BM))
         return PBM_ERR_INVALID;
     if (c->block_size < 0 || c->block_size > 256 || (c->block_size % 32) != 0) return PBM_ERR_INVALID;
     if (c->strategy != PBM_RANDOM_WALK && c->strategy != PBM_RANDOM_WALK_BM && c->strategy != PBM_COLLAB_RW_BM)

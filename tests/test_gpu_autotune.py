@@ -27,7 +27,7 @@ def test_autotune_ranks_candidates_and_keeps_occupancy(cuda, pbm_mod, orc):
     tab["offset"] = np.concatenate([[0], np.cumsum(counts)[:-1]])
     d_tab = torch.from_numpy(tab.view(np.uint8).copy()).cuda()
     res = pool.autotune(d_tab, 64, int(counts.sum()), arena, H, reps=2)
-    assert len(res) == 2 * (1 + 2 + 12) + 2
+    assert len(res) == 2 * (1 + 2 + 16) + 2
     rates = [r.ops_per_s for r in res]
     assert all(r > 0 for r in rates) and rates == sorted(rates, reverse=True)
     kinds = {(r.cfg.strategy, r.cfg.word_bits, r.cfg.collab_width, r.cfg.stride, r.cfg.blocks_per_sm,

@@ -28,7 +28,8 @@ def _descs(counts, op, start=0, arena_len=1 << 62):
 
 
 @pytest.mark.parametrize("mode", ["plain", "persistent", "graph"])
-@pytest.mark.parametrize("strategy,W,wb", [(2, 32, 32), (2, 16, 64), (1, 32, 32), (0, 32, 32)])
+@pytest.mark.parametrize("strategy,W,wb", [(2, 32, 32), (2, 16, 64), (2, 64, 32), (2, 64, 64), (1, 32, 32),
+                                           (0, 32, 32)])
 def test_swap_keeps_occupancy(cuda, pbm_mod, orc, mode, strategy, W, wb):
     torch = cuda
     pbm = pbm_mod

@@ -56,10 +56,10 @@ SEED0 = 1000
 METRIC = "alloc+free ops/s at 90% occupancy (batched persistent kernel, CUDA-graph replay)"
 UNIT = "ops/s"
 # DRAM bytes per alloc+free pair of the batch kernel: dram__bytes_read.sum +
-# dram__bytes_write.sum of one captured launch (7.81 MB for the 1,420,753-pair
-# step of `bench.py --profile`), summarised in
+# dram__bytes_write.sum of one captured launch (7.82 MB for the 1,420,753-pair
+# step of `bench.py --profile --profile-walk pair32c`), summarised in
 # profiles/batch_persistent_collab32_90pct.md.
-NCU_DRAM_BYTES_PER_PAIR = 7.810304e6 / 1420753
+NCU_DRAM_BYTES_PER_PAIR = 7.817984e6 / 1420753
 
 
 def env_rank():
@@ -431,7 +431,7 @@ def run_ours(args, rank, world, local_rank):
         "frac": atomic_achieved / ceil_ops, "traffic": traffic,
         "peak_source": "pbm_atomic_ceiling, spread pattern (uncontended atomicOr, 32 lanes on 32 lines), same run",
         "line_pattern_peak": ceil_line / 1e9, "frac_of_line_pattern": atomic_achieved / ceil_line,
-        "kernel": "k_batch_persistent<Collab,32,u32,5>: one launch per graph replay",
+        "kernel": "k_batch_persistent of the tuned walk (see tuned_config): one launch per graph replay",
         "hbm": {"achieved": hbm_achieved, "peak": hbm_peak, "unit": "GB/s", "frac": hbm_achieved / hbm_peak,
                 "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)" if peaks else "fallback"},
     }

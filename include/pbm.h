@@ -211,6 +211,15 @@ int pbm_gather_pages(pbm_pool *pool, const int32_t *d_ids, uint32_t n, uint32_t 
 int pbm_batch_launch(pbm_pool *pool, const pbm_walk_config *cfg, const pbm_group *d_groups,
                      const pbm_group *h_groups, uint32_t n_groups, int32_t *d_arena,
                      uint64_t arena_len, uint32_t seed, int32_t *d_steps, int mode, void *stream);
+/* The same, also writing each request's result to results[q] (request
+ * order q = 0 .. total-1): the new page of an ALLOC or SWAP (-1 if none was
+ * found), the page a FREE released.  `results` may be host memory mapped into
+ * the device (pinned, e.g. cudaHostAlloc): the kernel then streams the step's
+ * results to the host over the chip-to-chip link while it runs, with no
+ * separate device-to-host copy.  (No reference counterpart.) */
+int pbm_batch_launch_results(pbm_pool *pool, const pbm_walk_config *cfg, const pbm_group *d_groups,
+                             const pbm_group *h_groups, uint32_t n_groups, int32_t *d_arena, uint64_t arena_len,
+                             uint32_t seed, int32_t *d_steps, int32_t *results, int mode, void *stream);
 
 /* Graph-replayed persistent batch.  Replay k reads the descriptors at
  * d_groups + (k mod n_steps)*n_groups with seed seed0 + k, where k is a

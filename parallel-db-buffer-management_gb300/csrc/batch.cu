@@ -34,6 +34,7 @@ struct BatchArgs {
     int32_t* arena;
     unsigned long long arena_len;
     int32_t* steps;                     // parallel to arena, may be null
+    int32_t* results;                   // per request q (request order), may be null or host-mapped
     const unsigned long long* prefix;   // persistent, not fused: n_groups + 1 exclusive prefix
     int32_t fuse;                       // persistent: each block scans the groups itself
     uint32_t* done;                     // graph form: blocks finished (last one advances d_step)
@@ -63,10 +64,12 @@ __device__ __forceinline__ void flush_bacc(const BAcc& a, DevStats* st) {
 
 // The request's result: arena update, counters, and the free of the page it
 // gave up (merged per word within the warp when asked); converged call.
-__device__ __forceinline__ void batch_finish(const BatchArgs& a, bool active, int op, unsigned long long slot,
-                                             int32_t held, bool need, int32_t id, int32_t s, BAcc& acc) {
+__device__ __forceinline__ void batch_finish(const BatchArgs& a, bool active, int op, unsigned long long q,
+                                             unsigned long long slot, int32_t held, bool need, int32_t id, int32_t s,
+                                             BAcc& acc) {
     int32_t to_free = -1;
     if (active) {
+        if (a.results) a.results[q] = op == PBM_OP_FREE ? held : id;
         if (op == PBM_OP_ALLOC) {
             a.arena[slot] = id;
         } else if (op == PBM_OP_FREE) {
@@ -107,7 +110,7 @@ __device__ __forceinline__ void batch_round(const BatchArgs& a, uint32_t seed, b
         else if constexpr (K == BWalk::Word32) id = walk_word<uint32_t>(a.v, seed0, a.max_steps, &s);
         else id = walk_word<uint64_t>(a.v, seed0, a.max_steps, &s);
     }
-    batch_finish(a, active, op, slot, held, need, id, s, acc);
+    batch_finish(a, active, op, q, slot, held, need, id, s, acc);
 }
 
 // Two requests per lane (a: q0 + lane, b: q0 + 32 + lane), one walk.
@@ -122,8 +125,8 @@ __device__ __forceinline__ void batch_round2(const BatchArgs& a, uint32_t seed, 
     int32_t s = 0, id_a = -1, id_b = -1;
     walk_collab2<Word>(a.v, need_a, need_b, request_seed(seed, (uint32_t)q0), lane_off, a.dedupe != 0,
                        a.max_steps, id_a, id_b, &s);
-    batch_finish(a, act_a, op_a, slot_a, held_a, need_a, id_a, s, acc);
-    batch_finish(a, act_b, op_b, slot_b, held_b, need_b, id_b, s, acc);
+    batch_finish(a, act_a, op_a, q0 + (threadIdx.x & 31u), slot_a, held_a, need_a, id_a, s, acc);
+    batch_finish(a, act_b, op_b, q0 + 32u + (threadIdx.x & 31u), slot_b, held_b, need_b, id_b, s, acc);
 }
 
 __device__ __forceinline__ unsigned long long wrap_slot(unsigned long long slot, unsigned long long len) {
@@ -405,9 +408,9 @@ int valid_cfg(const pbm_walk_config* c) {
 
 extern "C" {
 
-int pbm_batch_launch(pbm_pool* pool, const pbm_walk_config* cfg, const pbm_group* d_groups,
-                     const pbm_group* h_groups, uint32_t n_groups, int32_t* d_arena,
-                     uint64_t arena_len, uint32_t seed, int32_t* d_steps, int mode, void* stream) {
+int pbm_batch_launch_results(pbm_pool* pool, const pbm_walk_config* cfg, const pbm_group* d_groups,
+                             const pbm_group* h_groups, uint32_t n_groups, int32_t* d_arena, uint64_t arena_len,
+                             uint32_t seed, int32_t* d_steps, int32_t* results, int mode, void* stream) {
     if (!pool || !d_arena || arena_len == 0) return PBM_ERR_INVALID;
     int rc = valid_cfg(cfg);
     if (rc) return rc;
@@ -415,6 +418,7 @@ int pbm_batch_launch(pbm_pool* pool, const pbm_walk_config* cfg, const pbm_group
     cudaStream_t s = (cudaStream_t)stream;
     pool->fifo_valid = false;
     BatchArgs a = base_args(pool, cfg, d_arena, arena_len, seed, d_steps);
+    a.results = results;
     if (mode == PBM_LAUNCH_PLAIN) {
         if (!h_groups) return PBM_ERR_INVALID;
         unsigned long long q = 0;
@@ -455,6 +459,13 @@ int pbm_batch_launch(pbm_pool* pool, const pbm_walk_config* cfg, const pbm_group
     a.n_groups = n_groups;
     a.prefix = pool->d_prefix;
     return launch_batch(cfg, a, true, s);
+}
+
+int pbm_batch_launch(pbm_pool* pool, const pbm_walk_config* cfg, const pbm_group* d_groups,
+                     const pbm_group* h_groups, uint32_t n_groups, int32_t* d_arena,
+                     uint64_t arena_len, uint32_t seed, int32_t* d_steps, int mode, void* stream) {
+    return pbm_batch_launch_results(pool, cfg, d_groups, h_groups, n_groups, d_arena, arena_len, seed, d_steps,
+                                    nullptr, mode, stream);
 }
 
 int pbm_batch_graph_create(pbm_pool* pool, const pbm_walk_config* cfg, const pbm_group* d_groups,

@@ -162,6 +162,8 @@ SIGNATURES = [
     ("pbm_gather_pages", c_int, [c_void_p, c_void_p, c_uint32, c_uint32, c_void_p, c_void_p]),
     ("pbm_batch_launch", c_int, [c_void_p, POINTER(WalkConfig), c_void_p, POINTER(Group), c_uint32,
                                  c_void_p, c_uint64, c_uint32, c_void_p, c_int, c_void_p]),
+    ("pbm_batch_launch_results", c_int, [c_void_p, POINTER(WalkConfig), c_void_p, POINTER(Group), c_uint32,
+                                         c_void_p, c_uint64, c_uint32, c_void_p, c_void_p, c_int, c_void_p]),
     ("pbm_batch_graph_create", c_int, [c_void_p, POINTER(WalkConfig), c_void_p, c_uint32, c_uint32,
                                        c_void_p, c_uint64, c_uint32, c_void_p, POINTER(c_void_p)]),
     ("pbm_graph_replay", c_int, [c_void_p, c_void_p]),
@@ -367,7 +369,13 @@ class Pool:
                                                                     _ptr(out), stream))
 
     def batch(self, cfg: WalkConfig, d_groups, h_groups, n_groups, arena, arena_len, seed, mode,
-              steps=None, stream=0):
+              steps=None, stream=0, results=None):
+        """results: per-request output (device memory or pinned host memory)."""
+        if results is not None:
+            return _check("pbm_batch_launch_results",
+                          self.lib.pbm_batch_launch_results(self.h, byref(cfg), _ptr(d_groups), h_groups, n_groups,
+                                                            _ptr(arena), arena_len, seed, _ptr(steps), _ptr(results),
+                                                            mode, stream))
         return _check("pbm_batch_launch",
                       self.lib.pbm_batch_launch(self.h, byref(cfg), _ptr(d_groups), h_groups, n_groups,
                                                 _ptr(arena), arena_len, seed, _ptr(steps), mode, stream))

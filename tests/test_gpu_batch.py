@@ -158,3 +158,57 @@ def test_single_group_persistent_matches_oracle(cuda, pbm_mod, orc):
         assert set(got[c:c + 32]) == set(exp[c:c + 32])
     assert np.array_equal(pool.read_bitmap(), words)
     pool.close()
+
+
+@pytest.mark.parametrize("where", ["device", "pinned_host"])
+def test_batch_results_buffer(cuda, pbm_mod, orc, where):
+    """pbm_batch_launch_results writes request q's result to results[q]: the
+    new page of an ALLOC or SWAP, the page a FREE released; into device memory
+    or into pinned host memory the kernel writes directly."""
+    torch = cuda
+    pbm = pbm_mod
+    T, occ, seed = 1 << 20, 0.9, 2
+    pool = pbm.Pool(T, 64)
+    pool.prefill(occ, seed)
+    words, held = _held_arena(orc, T, occ, seed)
+    H = len(held)
+    arena = torch.from_numpy(held).cuda()
+    counts = [5000, 1, 64, 3000, 777]
+    ops = [pbm.OP_SWAP, pbm.OP_SWAP, pbm.OP_FREE, pbm.OP_SWAP, pbm.OP_FREE]
+    tab = _descs(counts, ops)
+    N = sum(counts)
+    if where == "device":
+        res = torch.full((N,), -9, dtype=torch.int32, device="cuda")
+    else:
+        res = torch.full((N,), -9, dtype=torch.int32).pin_memory()
+    before = arena.cpu().numpy().copy()
+    for cfg in (pbm.walk_config(pbm.COLLAB_RW_BM, collab_width=64), pbm.walk_config(pbm.COLLAB_RW_BM)):
+        before = arena.cpu().numpy().copy()
+        pool.batch(cfg, torch.from_numpy(tab.view(np.uint8).copy()).cuda(), None, len(counts), arena, H, 77,
+                   pbm.LAUNCH_PERSISTENT, results=res)
+        torch.cuda.synchronize()
+        r = res.cpu().numpy() if where == "device" else res.numpy()
+        after = arena.cpu().numpy()
+        q = 0
+        for c, op in zip(counts, ops):
+            if op == pbm.OP_FREE:
+                assert np.array_equal(r[q:q + c], before[q:q + c])       # the released pages
+            else:
+                assert np.array_equal(r[q:q + c], after[q:q + c])        # the new pages
+            q += c
+        # restore the released slots' pages so the next round starts from a full arena
+        freed = np.concatenate([before[sum(counts[:i]):sum(counts[:i + 1])] for i, o in enumerate(ops)
+                                if o == pbm.OP_FREE])
+        ids = torch.from_numpy(freed.astype(np.int32)).cuda()
+        st = torch.zeros(len(freed), dtype=torch.int32, device="cuda")
+        n = len(freed)
+        pool.alloc(pbm.walk_config(pbm.COLLAB_RW_BM), n, 5, ids)
+        q = 0
+        for c, op in zip(counts, ops):
+            if op == pbm.OP_FREE:
+                arena[q:q + c] = ids[:c]
+                ids = ids[c:]
+            q += c
+    chk = pool.check(arena, H)
+    assert chk.n_duplicates == 0 and chk.n_not_marked == 0 and chk.used_pages == H
+    pool.close()

@@ -59,20 +59,36 @@ struct BmView {
     int32_t dist;            // 0 = single hand, 1 = per-slot hands
 };
 
-__device__ __forceinline__ uint32_t next_frame(const BmView& b, uint32_t slot, uint32_t* arm_local) {
-    if (!b.dist) return (uint32_t)(atomicAdd(b.single_hand, 1ull) % b.n_frames);
-    uint32_t a = *arm_local;
-    uint32_t f = a >= b.n_frames ? a - b.n_frames : a;
-    *arm_local = f + 1u;
-    return f;
-}
+// Shared-hand positions a sweeping thread takes per atomic in parallel rounds.
+// Measured on the Zipf(0.99) trace: 8 raised fetches/s by 20% but dropped the
+// hit rate from 85.2% to 82.1% (positions reserved past the victim are
+// skipped, so the hand laps faster than frames are examined) and slowed the
+// 4 KiB-copy form by 37%; 2 kept the hit rate and gained nothing.  So the
+// hand moves one position per atomic, as the reference's SingleClock arm.
+constexpr uint32_t kHandBatch = 1;
 
 // Victim search; returns a frame now holding (page, 1 pin) and its old page.
-__device__ __forceinline__ int32_t sweep(const BmView& b, uint32_t page, uint32_t slot, uint32_t* old_page) {
+// The shared hand advances `batch` positions per atomic, which the sweeping
+// thread then examines in order (parallelPage.cu:491-509 steps it by one).
+__device__ __forceinline__ int32_t sweep(const BmView& b, uint32_t page, uint32_t slot, uint32_t batch,
+                                         uint32_t* old_page) {
     uint32_t arm = b.dist ? b.arms[slot] : 0u;
+    unsigned long long res = 0;
+    uint32_t res_left = 0;
     int32_t out = -1;
     for (uint32_t i = 0; i < b.max_sweep; ++i) {
-        uint32_t f = next_frame(b, slot, &arm);
+        uint32_t f;
+        if (b.dist) {
+            f = arm >= b.n_frames ? arm - b.n_frames : arm;
+            arm = f + 1u;
+        } else {
+            if (res_left == 0u) {
+                res = atomicAdd(b.single_hand, (unsigned long long)batch);
+                res_left = batch;
+            }
+            f = (uint32_t)((res + (batch - res_left)) % b.n_frames);
+            --res_left;
+        }
         unsigned long long s = __ldcg(b.frame_state + f);
         if ((uint32_t)s != 0u) continue;                    // pinned
         if (b.ref[f]) { b.ref[f] = 0; continue; }           // second chance
@@ -100,7 +116,7 @@ __device__ __forceinline__ bool pin_if_owner(const BmView& b, int32_t f, uint32_
     return false;
 }
 
-__device__ __forceinline__ int32_t fetch(const BmView& b, uint32_t page, uint32_t slot, BmAcc& acc) {
+__device__ __forceinline__ int32_t fetch(const BmView& b, uint32_t page, uint32_t slot, uint32_t batch, BmAcc& acc) {
     for (uint32_t attempt = 0; attempt < kFetchSpinLimit; ++attempt) {
         int32_t f = __ldcg(b.page_table + page);
         if (f >= 0) {
@@ -114,7 +130,7 @@ __device__ __forceinline__ int32_t fetch(const BmView& b, uint32_t page, uint32_
         if (f == -1) {
             if (atomicCAS(b.page_table + page, -1, kLoading) != -1) continue;
             uint32_t old_page = kEmptyPage;
-            int32_t h = sweep(b, page, slot, &old_page);
+            int32_t h = sweep(b, page, slot, batch, &old_page);
             if (h < 0) {
                 atomicExch(b.page_table + page, -1);
                 ++acc.failures;
@@ -141,16 +157,20 @@ __device__ __forceinline__ int32_t fetch(const BmView& b, uint32_t page, uint32_
     return -1;
 }
 
-__device__ __forceinline__ void unpin(const BmView& b, int32_t f, unsigned long long& ok, unsigned long long& bad) {
-    if (f < 0 || (uint32_t)f >= b.n_frames) return;
-    if ((uint32_t)__ldcg(b.frame_state + f) == 0u) { ++bad; return; }   // nothing pinned
-    const unsigned long long old = atomicAdd(b.frame_state + f, ~0ull);
-    if ((uint32_t)old == 0u) {          // a racing unpin of the same pin took it first
-        atomicAdd(b.frame_state + f, 1ull);
-        ++bad;
+// Releases k pins of frame f with one atomic.  A release of more pins than
+// the frame holds (a caller error) is taken back and counted as bad; its
+// subtraction can borrow from the page field for that instant, which makes a
+// racing fetch see another page and retry, and a racing sweep's CAS fail.
+__device__ __forceinline__ void unpin_k(const BmView& b, int32_t f, uint32_t k, unsigned long long& ok,
+                                        unsigned long long& bad) {
+    if (f < 0 || (uint32_t)f >= b.n_frames || k == 0u) return;
+    const unsigned long long old = atomicAdd(b.frame_state + f, 0ull - (unsigned long long)k);
+    if ((uint32_t)old < k) {
+        atomicAdd(b.frame_state + f, (unsigned long long)k);
+        bad += k;
         return;
     }
-    ++ok;
+    ok += k;
 }
 
 // One round: release the listed pins, then fetch this round's pages.
@@ -162,9 +182,19 @@ __global__ void __launch_bounds__(256) k_round(BmView b, const int32_t* release_
     const uint32_t tid = blockIdx.x * blockDim.x + threadIdx.x;
     const uint32_t nthr = gridDim.x * blockDim.x;
     unsigned long long ok = 0, bad = 0;
-    for (uint32_t j = tid; j < n_release; j += nthr) {
-        int32_t idx = release_idx[j];
-        unpin(b, release_frames_of[idx], ok, bad);
+    if (nthr == 1u) {
+        for (uint32_t j = 0; j < n_release; ++j) unpin_k(b, release_frames_of[release_idx[j]], 1u, ok, bad);
+    } else {
+        // warp-uniform trip count: lanes releasing pins of the same frame (hot
+        // pages of a skewed stream) merge them into one atomic
+        const uint32_t lane = threadIdx.x & 31u;
+        for (uint32_t base = tid - lane; base < n_release; base += nthr) {
+            const uint32_t j = base + lane;
+            const int32_t f = j < n_release ? release_frames_of[release_idx[j]] : -1;
+            const bool valid = f >= 0 && (uint32_t)f < b.n_frames;
+            const uint32_t peers = __match_any_sync(0xffffffffu, valid ? (uint32_t)f : 0x80000000u + lane);
+            if (valid && (uint32_t)(__ffs((int)peers) - 1) == lane) unpin_k(b, f, (uint32_t)__popc(peers), ok, bad);
+        }
     }
     BmAcc acc;
     if (nthr == 1u) {
@@ -172,7 +202,7 @@ __global__ void __launch_bounds__(256) k_round(BmView b, const int32_t* release_
         for (uint32_t i = 0; i < n; ++i) {
             int32_t p = pages[i];
             int32_t f = -1;
-            if (p >= 0 && (uint32_t)p < b.n_logical) f = fetch(b, (uint32_t)p, (slot0 + i) % b.n_arms, acc);
+            if (p >= 0 && (uint32_t)p < b.n_logical) f = fetch(b, (uint32_t)p, (slot0 + i) % b.n_arms, 1u, acc);
             frames_out[i] = f;
         }
     } else {
@@ -200,7 +230,7 @@ __global__ void __launch_bounds__(256) k_round(BmView b, const int32_t* release_
                 f = hit;
                 ++acc.hits;
             } else if (valid) {
-                f = fetch(b, (uint32_t)p, (slot0 + i) % b.n_arms, acc);
+                f = fetch(b, (uint32_t)p, (slot0 + i) % b.n_arms, kHandBatch, acc);
             }
             if (i < n) frames_out[i] = f;
         }

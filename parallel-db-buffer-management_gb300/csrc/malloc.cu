@@ -7,6 +7,7 @@
 // Reference: mallocRW / freeRW (source/RWMalloc.cuh:299-334), the
 // KernelMallocCollab allocator (source/malloc.cu:223-320) and the
 // malloc/free drivers (unitTests/unitTest3.cu, unitTestMalloc1.cu).
+#include <mutex>
 #include <new>
 
 #include "batch_common.cuh"
@@ -172,7 +173,10 @@ using namespace pbm;
 
 namespace {
 
-// Malloc tables of a pool live beside it, keyed by the pool handle.
+// Malloc tables of a pool live beside it, keyed by the pool handle.  Every
+// entry point takes g_reg_mu for its whole call (launches only enqueue work),
+// so tables are never moved or freed under another thread's call.
+std::mutex g_reg_mu;
 struct Registry {
     pbm_pool* pool;
     MallocTables t;
@@ -400,6 +404,7 @@ int graph_impl(pbm_pool* pool, bool queue, const pbm_group* d_groups, uint32_t n
 extern "C" {
 
 int pbm_malloc_init(pbm_pool* pool) {
+    std::lock_guard<std::mutex> lk(g_reg_mu);
     int rc = check_pool(pool);
     if (rc) return rc;
     MallocTables* t = tables_add(pool);
@@ -424,6 +429,7 @@ int pbm_malloc_init(pbm_pool* pool) {
 }
 
 int pbm_malloc_tables(pbm_pool* pool, void** d_start_of, void** d_live, void** d_len_of) {
+    std::lock_guard<std::mutex> lk(g_reg_mu);
     MallocTables* t = tables_of(pool);
     if (!t || !t->start_of) return PBM_ERR_INVALID;
     if (d_start_of) *d_start_of = t->start_of;
@@ -433,6 +439,7 @@ int pbm_malloc_tables(pbm_pool* pool, void** d_start_of, void** d_live, void** d
 }
 
 int pbm_malloc_release(pbm_pool* pool) {
+    std::lock_guard<std::mutex> lk(g_reg_mu);
     MallocTables* t = tables_of(pool);
     if (!t) return PBM_ERR_INVALID;
     cudaDeviceSynchronize();
@@ -450,6 +457,7 @@ int pbm_malloc_release(pbm_pool* pool) {
 int pbm_malloc_batch(pbm_pool* pool, const pbm_group* d_groups, const pbm_group* h_groups, uint32_t n_groups,
                      const uint32_t* d_sizes, unsigned long long* d_ptrs, uint64_t arena_len, uint32_t seed,
                      uint32_t max_steps, int mode, void* stream) {
+    std::lock_guard<std::mutex> lk(g_reg_mu);
     return batch_impl(pool, false, d_groups, h_groups, n_groups, d_sizes, d_ptrs, arena_len, seed, max_steps, mode,
                       stream);
 }
@@ -457,11 +465,13 @@ int pbm_malloc_batch(pbm_pool* pool, const pbm_group* d_groups, const pbm_group*
 int pbm_malloc_graph_create(pbm_pool* pool, const pbm_group* d_groups, uint32_t n_groups, uint32_t n_steps,
                             const uint32_t* d_sizes, unsigned long long* d_ptrs, uint64_t arena_len,
                             uint32_t seed0, uint32_t max_steps, void* stream, pbm_graph** out) {
+    std::lock_guard<std::mutex> lk(g_reg_mu);
     return graph_impl(pool, false, d_groups, n_groups, n_steps, d_sizes, d_ptrs, arena_len, seed0, max_steps, stream,
                       out);
 }
 
 int pbm_malloc_counts(pbm_pool* pool, uint64_t* h_live_runs, uint64_t* h_bad_frees, void* stream) {
+    std::lock_guard<std::mutex> lk(g_reg_mu);
     MallocTables* t = tables_of(pool);
     if (!t || !t->start_of) return PBM_ERR_INVALID;
     cudaStream_t s = (cudaStream_t)stream;
@@ -487,6 +497,7 @@ int pbm_malloc_counts(pbm_pool* pool, uint64_t* h_live_runs, uint64_t* h_bad_fre
 // ---- queue backend ----
 
 int pbm_qmalloc_init(pbm_pool* pool, uint32_t ring_capacity) {
+    std::lock_guard<std::mutex> lk(g_reg_mu);
     int rc = check_pool(pool);
     if (rc) return rc;
     if (pool->n_pages * (uint64_t)pool->page_size > (1ull << 36)) return PBM_ERR_INVALID;   // 32-bit handles of 16 B
@@ -516,6 +527,7 @@ int pbm_qmalloc_init(pbm_pool* pool, uint32_t ring_capacity) {
 }
 
 int pbm_qmalloc_release(pbm_pool* pool) {
+    std::lock_guard<std::mutex> lk(g_reg_mu);
     MallocTables* t = tables_of(pool);
     if (!t || !t->rings) return PBM_ERR_INVALID;
     cudaDeviceSynchronize();
@@ -527,6 +539,7 @@ int pbm_qmalloc_release(pbm_pool* pool) {
 int pbm_qmalloc_batch(pbm_pool* pool, const pbm_group* d_groups, const pbm_group* h_groups, uint32_t n_groups,
                       const uint32_t* d_sizes, unsigned long long* d_ptrs, uint64_t arena_len, uint32_t seed,
                       uint32_t max_steps, int mode, void* stream) {
+    std::lock_guard<std::mutex> lk(g_reg_mu);
     return batch_impl(pool, true, d_groups, h_groups, n_groups, d_sizes, d_ptrs, arena_len, seed, max_steps, mode,
                       stream);
 }
@@ -534,12 +547,14 @@ int pbm_qmalloc_batch(pbm_pool* pool, const pbm_group* d_groups, const pbm_group
 int pbm_qmalloc_graph_create(pbm_pool* pool, const pbm_group* d_groups, uint32_t n_groups, uint32_t n_steps,
                              const uint32_t* d_sizes, unsigned long long* d_ptrs, uint64_t arena_len,
                              uint32_t seed0, uint32_t max_steps, void* stream, pbm_graph** out) {
+    std::lock_guard<std::mutex> lk(g_reg_mu);
     return graph_impl(pool, true, d_groups, n_groups, n_steps, d_sizes, d_ptrs, arena_len, seed0, max_steps, stream,
                       out);
 }
 
 int pbm_qmalloc_counts(pbm_pool* pool, uint64_t* h_queued, uint64_t* h_chunks, uint64_t* h_overflow,
                        uint64_t* h_timeouts, uint64_t* h_bad_frees, void* stream) {
+    std::lock_guard<std::mutex> lk(g_reg_mu);
     MallocTables* t = tables_of(pool);
     if (!t || !t->rings) return PBM_ERR_INVALID;
     cudaStream_t s = (cudaStream_t)stream;

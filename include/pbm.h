@@ -207,7 +207,12 @@ int pbm_gather_pages(pbm_pool *pool, const int32_t *d_ids, uint32_t n, uint32_t 
  * descriptors; h_groups: the same descriptors in host memory (needed by the
  * plain form, which launches one kernel per group; may be NULL for the
  * persistent form).  d_arena: id arena of arena_len slots.  The persistent
- * form is a single launch and can be captured in a CUDA graph. */
+ * form is a single launch and can be captured in a CUDA graph.
+ * Persistent form with d_groups NULL: the host table h_groups (at most
+ * PBM_MAX_INLINE_GROUPS groups) is copied into the launch's parameters, so the
+ * step needs no separate host-to-device copy; h_groups may be reused as soon
+ * as the call returns. */
+#define PBM_MAX_INLINE_GROUPS 256
 int pbm_batch_launch(pbm_pool *pool, const pbm_walk_config *cfg, const pbm_group *d_groups,
                      const pbm_group *h_groups, uint32_t n_groups, int32_t *d_arena,
                      uint64_t arena_len, uint32_t seed, int32_t *d_steps, int mode, void *stream);
@@ -229,6 +234,11 @@ typedef struct pbm_graph pbm_graph;
 int pbm_batch_graph_create(pbm_pool *pool, const pbm_walk_config *cfg, const pbm_group *d_groups,
                            uint32_t n_groups, uint32_t n_steps, int32_t *d_arena,
                            uint64_t arena_len, uint32_t seed0, void *stream, pbm_graph **out);
+/* The graph form of pbm_batch_launch_results: each replay also writes its
+ * step's results to results[q] (device or pinned host memory). */
+int pbm_batch_graph_create_results(pbm_pool *pool, const pbm_walk_config *cfg, const pbm_group *d_groups,
+                                   uint32_t n_groups, uint32_t n_steps, int32_t *d_arena, uint64_t arena_len,
+                                   uint32_t seed0, int32_t *results, void *stream, pbm_graph **out);
 int pbm_graph_replay(pbm_graph *g, void *stream);
 int pbm_graph_set_step(pbm_graph *g, uint32_t step, void *stream);
 int pbm_graph_destroy(pbm_graph *g);

@@ -14,6 +14,8 @@
 //               block to finish advances the device-resident step counter, so
 //               each replay is one launch that reads the next step's
 //               descriptors from device memory.
+#include <type_traits>
+
 #include "batch_common.cuh"
 
 namespace pbm {
@@ -49,6 +51,15 @@ struct BatchArgs {
     unsigned long long offset;
     unsigned long long q_base;
 };
+
+// The launch form may carry the step's descriptors in the kernel's parameter
+// block (a host table of at most PBM_MAX_INLINE_GROUPS groups): the table then
+// travels with the launch itself and a host-driven step needs no separate
+// host-to-device copy.  NoTable is the empty parameter of the other forms.
+struct GroupTable {
+    pbm_group g[PBM_MAX_INLINE_GROUPS];
+};
+struct NoTable {};
 
 // Per-thread counters of a launch; ok / fail / frees count requests of the
 // thread (at most one per chunk it serves), steps may pass 2^32.
@@ -161,8 +172,8 @@ __device__ __forceinline__ uint32_t find_group_warp(const unsigned long long* pr
 // back (static striding left the slowest of ~8 chunks per warp as the tail).
 // (Prefetching the next chunk's arena slots and bitmap line into L2 was
 // measured slower: the extra instructions cost more than the latency they hid.)
-template <BWalk K, int W, typename Word, int MINB>
-__global__ void __launch_bounds__(256, MINB) k_batch_persistent(BatchArgs a) {
+template <BWalk K, int W, typename Word, int MINB, typename Tab>
+__global__ void __launch_bounds__(256, MINB) k_batch_persistent(BatchArgs a, const __grid_constant__ Tab tab) {
     extern __shared__ unsigned long long s_prefix[];
     __shared__ int32_t slots[256];
     __shared__ bool s_last;
@@ -170,7 +181,9 @@ __global__ void __launch_bounds__(256, MINB) k_batch_persistent(BatchArgs a) {
     BAcc acc;
     if (threadIdx.x == 0) s_next_chunk = 0u;
     const uint32_t step = a.d_step ? *a.d_step : 0u;
-    const pbm_group* groups = a.groups + (a.d_step ? (size_t)(step % a.n_steps) * a.n_groups : 0);
+    const pbm_group* groups;
+    if constexpr (std::is_same<Tab, GroupTable>::value) groups = tab.g;   // read in place
+    else groups = a.groups + (a.d_step ? (size_t)(step % a.n_steps) * a.n_groups : 0);
     const uint32_t seed = a.seed + step;
     const unsigned long long* pre = a.prefix;
     if (a.fuse) {
@@ -275,12 +288,12 @@ namespace {
 
 // Resident blocks per SM of a persistent instantiation (queried once per block
 // size, outside any stream capture).
-template <BWalk K, int W, typename Word, int MINB>
+template <BWalk K, int W, typename Word, int MINB, typename Tab = NoTable>
 int persistent_blocks_per_sm(int block) {
     static int cached_block = 0, cached = 0;
     if (cached_block != block) {
         int n = 0;
-        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_batch_persistent<K, W, Word, MINB>, block, kFusedPrefixBytes) !=
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_batch_persistent<K, W, Word, MINB, Tab>, block, kFusedPrefixBytes) !=
             cudaSuccess) {
             cudaGetLastError();
             n = 1;
@@ -296,19 +309,28 @@ int persistent_blocks_per_sm(int block) {
 // >= kCappedBlocks: the variant whose registers are capped for kCappedBlocks
 // resident blocks (5 x 256 threads: at most 51 registers, no spills for the
 // collaborative walk on 32-bit words).
+template <BWalk K, int W, typename Word, typename Tab>
+void launch_persistent(const BatchArgs& a, const Tab& tab, int block, int blocks_per_sm, size_t smem,
+                       cudaStream_t s) {
+    if (blocks_per_sm >= kCappedBlocks) {
+        int fit = persistent_blocks_per_sm<K, W, Word, kCappedBlocks, Tab>(block);
+        int per_sm = blocks_per_sm < fit ? blocks_per_sm : fit;
+        k_batch_persistent<K, W, Word, kCappedBlocks, Tab><<<sm_count() * per_sm, block, smem, s>>>(a, tab);
+    } else {
+        int fit = persistent_blocks_per_sm<K, W, Word, 1, Tab>(block);
+        int per_sm = (blocks_per_sm > 0 && blocks_per_sm < fit) ? blocks_per_sm : fit;
+        k_batch_persistent<K, W, Word, 1, Tab><<<sm_count() * per_sm, block, smem, s>>>(a, tab);
+    }
+}
+
+// tab: the inline descriptor table of a launch-form batch (null: a.groups).
 template <BWalk K, int W, typename Word>
-int launch_batch_kw(const BatchArgs& a, bool persistent, int block, int blocks_per_sm, cudaStream_t s) {
+int launch_batch_kw(const BatchArgs& a, bool persistent, int block, int blocks_per_sm, cudaStream_t s,
+                    const GroupTable* tab) {
     if (persistent) {
         const size_t smem = a.fuse ? sizeof(unsigned long long) * (a.n_groups + 1u) : 0u;
-        if (blocks_per_sm >= kCappedBlocks) {
-            int fit = persistent_blocks_per_sm<K, W, Word, kCappedBlocks>(block);
-            int per_sm = blocks_per_sm < fit ? blocks_per_sm : fit;
-            k_batch_persistent<K, W, Word, kCappedBlocks><<<sm_count() * per_sm, block, smem, s>>>(a);
-        } else {
-            int fit = persistent_blocks_per_sm<K, W, Word, 1>(block);
-            int per_sm = (blocks_per_sm > 0 && blocks_per_sm < fit) ? blocks_per_sm : fit;
-            k_batch_persistent<K, W, Word, 1><<<sm_count() * per_sm, block, smem, s>>>(a);
-        }
+        if (tab) launch_persistent<K, W, Word>(a, *tab, block, blocks_per_sm, smem, s);
+        else launch_persistent<K, W, Word>(a, NoTable{}, block, blocks_per_sm, smem, s);
     } else {
         const unsigned long long per_warp = 32ull * kReqPerLane<K>;
         unsigned long long warps = (a.count + per_warp - 1ull) / per_warp;
@@ -320,26 +342,27 @@ int launch_batch_kw(const BatchArgs& a, bool persistent, int block, int blocks_p
     return PBM_OK;
 }
 
-int launch_batch(const pbm_walk_config* c, const BatchArgs& a, bool persistent, cudaStream_t s) {
+int launch_batch(const pbm_walk_config* c, const BatchArgs& a, bool persistent, cudaStream_t s,
+                 const GroupTable* tab = nullptr) {
     const int block = c->block_size ? c->block_size : kDefaultBlock;
     const int bps = c->blocks_per_sm;
     const bool w64 = c->word_bits == 64;
     switch (c->strategy) {
     case PBM_RANDOM_WALK:
-        return launch_batch_kw<BWalk::Page, 32, uint32_t>(a, persistent, block, bps, s);
+        return launch_batch_kw<BWalk::Page, 32, uint32_t>(a, persistent, block, bps, s, tab);
     case PBM_RANDOM_WALK_BM:
-        return w64 ? launch_batch_kw<BWalk::Word64, 32, uint64_t>(a, persistent, block, bps, s)
-                   : launch_batch_kw<BWalk::Word32, 32, uint32_t>(a, persistent, block, bps, s);
+        return w64 ? launch_batch_kw<BWalk::Word64, 32, uint64_t>(a, persistent, block, bps, s, tab)
+                   : launch_batch_kw<BWalk::Word32, 32, uint32_t>(a, persistent, block, bps, s, tab);
     case PBM_COLLAB_RW_BM: {
         const int W = c->collab_width ? c->collab_width : 32;
-        if (W == 64) return w64 ? launch_batch_kw<BWalk::Collab2, 32, uint64_t>(a, persistent, block, bps, s)
-                                : launch_batch_kw<BWalk::Collab2, 32, uint32_t>(a, persistent, block, bps, s);
-        if (W == 8) return w64 ? launch_batch_kw<BWalk::Collab, 8, uint64_t>(a, persistent, block, bps, s)
-                               : launch_batch_kw<BWalk::Collab, 8, uint32_t>(a, persistent, block, bps, s);
-        if (W == 16) return w64 ? launch_batch_kw<BWalk::Collab, 16, uint64_t>(a, persistent, block, bps, s)
-                                : launch_batch_kw<BWalk::Collab, 16, uint32_t>(a, persistent, block, bps, s);
-        return w64 ? launch_batch_kw<BWalk::Collab, 32, uint64_t>(a, persistent, block, bps, s)
-                   : launch_batch_kw<BWalk::Collab, 32, uint32_t>(a, persistent, block, bps, s);
+        if (W == 64) return w64 ? launch_batch_kw<BWalk::Collab2, 32, uint64_t>(a, persistent, block, bps, s, tab)
+                                : launch_batch_kw<BWalk::Collab2, 32, uint32_t>(a, persistent, block, bps, s, tab);
+        if (W == 8) return w64 ? launch_batch_kw<BWalk::Collab, 8, uint64_t>(a, persistent, block, bps, s, tab)
+                               : launch_batch_kw<BWalk::Collab, 8, uint32_t>(a, persistent, block, bps, s, tab);
+        if (W == 16) return w64 ? launch_batch_kw<BWalk::Collab, 16, uint64_t>(a, persistent, block, bps, s, tab)
+                                : launch_batch_kw<BWalk::Collab, 16, uint32_t>(a, persistent, block, bps, s, tab);
+        return w64 ? launch_batch_kw<BWalk::Collab, 32, uint64_t>(a, persistent, block, bps, s, tab)
+                   : launch_batch_kw<BWalk::Collab, 32, uint32_t>(a, persistent, block, bps, s, tab);
     }
     default:
         return PBM_ERR_UNSUPPORTED;
@@ -436,7 +459,18 @@ int pbm_batch_launch_results(pbm_pool* pool, const pbm_walk_config* cfg, const p
         }
         return PBM_OK;
     }
-    if (mode != PBM_LAUNCH_PERSISTENT || !d_groups) return PBM_ERR_INVALID;
+    if (mode != PBM_LAUNCH_PERSISTENT) return PBM_ERR_INVALID;
+    if (!d_groups) {                   // host table carried in the launch's parameters
+        if (!h_groups || n_groups > PBM_MAX_INLINE_GROUPS) return PBM_ERR_INVALID;
+        GroupTable tab{};
+        for (uint32_t g = 0; g < n_groups; ++g) {
+            if (h_groups[g].op < PBM_OP_ALLOC || h_groups[g].op > PBM_OP_SWAP) return PBM_ERR_INVALID;
+            tab.g[g] = h_groups[g];
+        }
+        a.n_groups = n_groups;
+        a.fuse = 1;
+        return launch_batch(cfg, a, true, s, &tab);
+    }
     a.groups = d_groups;
     a.n_groups = n_groups;
     if (n_groups <= kFusedGroups) {   // every block scans the groups itself
@@ -471,6 +505,13 @@ int pbm_batch_launch(pbm_pool* pool, const pbm_walk_config* cfg, const pbm_group
 int pbm_batch_graph_create(pbm_pool* pool, const pbm_walk_config* cfg, const pbm_group* d_groups,
                            uint32_t n_groups, uint32_t n_steps, int32_t* d_arena, uint64_t arena_len,
                            uint32_t seed0, void* stream, pbm_graph** out) {
+    return pbm_batch_graph_create_results(pool, cfg, d_groups, n_groups, n_steps, d_arena, arena_len, seed0, nullptr,
+                                          stream, out);
+}
+
+int pbm_batch_graph_create_results(pbm_pool* pool, const pbm_walk_config* cfg, const pbm_group* d_groups,
+                                   uint32_t n_groups, uint32_t n_steps, int32_t* d_arena, uint64_t arena_len,
+                                   uint32_t seed0, int32_t* results, void* stream, pbm_graph** out) {
     if (!pool || !d_groups || !d_arena || !out || n_groups == 0 || n_steps == 0 || arena_len == 0)
         return PBM_ERR_INVALID;
     int rc = valid_cfg(cfg);
@@ -496,6 +537,7 @@ int pbm_batch_graph_create(pbm_pool* pool, const pbm_walk_config* cfg, const pbm
     PBM_CUDA_TRY(cudaMemsetAsync(g->d_done, 0, sizeof(uint32_t), s));
     PBM_CUDA_TRY(cudaStreamSynchronize(s));
     BatchArgs a = base_args(pool, cfg, d_arena, arena_len, seed0, nullptr);
+    a.results = results;
     a.groups = d_groups;
     a.n_groups = n_groups;
     a.prefix = g->d_prefix;

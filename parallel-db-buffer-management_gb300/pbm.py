@@ -44,6 +44,7 @@ STRATEGY_NAMES = {
 
 OP_ALLOC, OP_FREE, OP_SWAP, OP_MALLOC, OP_MFREE = 0, 1, 2, 3, 4
 LAUNCH_PLAIN, LAUNCH_PERSISTENT, LAUNCH_SERIAL = 0, 1, 2
+MAX_INLINE_GROUPS = 256           # PBM_MAX_INLINE_GROUPS
 POOL_MATERIALIZE = 1
 
 
@@ -166,6 +167,8 @@ SIGNATURES = [
                                          c_void_p, c_uint64, c_uint32, c_void_p, c_void_p, c_int, c_void_p]),
     ("pbm_batch_graph_create", c_int, [c_void_p, POINTER(WalkConfig), c_void_p, c_uint32, c_uint32,
                                        c_void_p, c_uint64, c_uint32, c_void_p, POINTER(c_void_p)]),
+    ("pbm_batch_graph_create_results", c_int, [c_void_p, POINTER(WalkConfig), c_void_p, c_uint32, c_uint32,
+                                               c_void_p, c_uint64, c_uint32, c_void_p, c_void_p, POINTER(c_void_p)]),
     ("pbm_graph_replay", c_int, [c_void_p, c_void_p]),
     ("pbm_graph_set_step", c_int, [c_void_p, c_uint32, c_void_p]),
     ("pbm_graph_destroy", c_int, [c_void_p]),
@@ -370,7 +373,12 @@ class Pool:
 
     def batch(self, cfg: WalkConfig, d_groups, h_groups, n_groups, arena, arena_len, seed, mode,
               steps=None, stream=0, results=None):
-        """results: per-request output (device memory or pinned host memory)."""
+        """results: per-request output (device memory or pinned host memory).
+        h_groups: a Group array, or a host tensor / address of packed descriptors.
+        Persistent mode with d_groups None carries h_groups (at most
+        MAX_INLINE_GROUPS) in the launch itself."""
+        if h_groups is not None and not isinstance(h_groups, ctypes.Array):
+            h_groups = ctypes.cast(ctypes.c_void_p(_ptr(h_groups)), POINTER(Group))
         if results is not None:
             return _check("pbm_batch_launch_results",
                           self.lib.pbm_batch_launch_results(self.h, byref(cfg), _ptr(d_groups), h_groups, n_groups,
@@ -380,11 +388,13 @@ class Pool:
                       self.lib.pbm_batch_launch(self.h, byref(cfg), _ptr(d_groups), h_groups, n_groups,
                                                 _ptr(arena), arena_len, seed, _ptr(steps), mode, stream))
 
-    def graph(self, cfg: WalkConfig, d_groups, n_groups, n_steps, arena, arena_len, seed0, stream=0):
+    def graph(self, cfg: WalkConfig, d_groups, n_groups, n_steps, arena, arena_len, seed0, stream=0,
+              results=None):
         g = c_void_p()
-        _check("pbm_batch_graph_create",
-               self.lib.pbm_batch_graph_create(self.h, byref(cfg), _ptr(d_groups), n_groups, n_steps,
-                                               _ptr(arena), arena_len, seed0, stream, byref(g)))
+        _check("pbm_batch_graph_create_results",
+               self.lib.pbm_batch_graph_create_results(self.h, byref(cfg), _ptr(d_groups), n_groups, n_steps,
+                                                       _ptr(arena), arena_len, seed0, _ptr(results), stream,
+                                                       byref(g)))
         return Graph(self.lib, g)
 
     # size-classed malloc -----------------------------------------------------------

@@ -212,3 +212,110 @@ def test_batch_results_buffer(cuda, pbm_mod, orc, where):
     chk = pool.check(arena, H)
     assert chk.n_duplicates == 0 and chk.n_not_marked == 0 and chk.used_pages == H
     pool.close()
+
+
+def test_graph_results_into_pinned_host(cuda, pbm_mod, orc):
+    """pbm_batch_graph_create_results: each replay reads the staging table
+    (refilled between replays) and writes its step's new pages into pinned
+    host memory."""
+    torch = cuda
+    pbm = pbm_mod
+    T, occ, seed = 1 << 20, 0.9, 2
+    pool = pbm.Pool(T, 64)
+    pool.prefill(occ, seed)
+    words, held = _held_arena(orc, T, occ, seed)
+    H = len(held)
+    arena = torch.from_numpy(held).cuda()
+    stage = torch.zeros(16 * 8, dtype=torch.uint8, device="cuda")
+    res = torch.full((40000,), -9, dtype=torch.int32).pin_memory()
+    g = pool.graph(pbm.walk_config(pbm.COLLAB_RW_BM, collab_width=64), stage, 8, 1, arena, H, 31, results=res)
+    rng = np.random.default_rng(9)
+    start = 0
+    for step in range(3):
+        counts = rng.integers(1, 5000, 8)
+        tab = _descs(counts, pbm.OP_SWAP, start, H)
+        stage.copy_(torch.from_numpy(tab.view(np.uint8).copy()))
+        g.replay()
+        torch.cuda.synchronize()
+        n = int(counts.sum())
+        a = arena.cpu().numpy()
+        idx = (start + np.arange(n)) % H
+        assert np.array_equal(res.numpy()[:n], a[idx])
+        start = (start + n) % H
+    g.close()
+    chk = pool.check(arena, H)
+    assert chk.n_duplicates == 0 and chk.n_not_marked == 0 and chk.used_pages == H
+    pool.close()
+
+
+def test_inline_table_launch(cuda, pbm_mod, orc):
+    """Persistent launch with the host descriptor table carried in the kernel's
+    parameters (d_groups NULL): the same oracle parity as a device table on a
+    sparse pool, request-ordered results and invariants on a mixed batch, and
+    tables that cannot be carried inline are rejected."""
+    torch = cuda
+    pbm = pbm_mod
+    cfg = pbm.walk_config(pbm.COLLAB_RW_BM)
+    # parity: one ALLOC group on a pool where no two warps race for a word
+    T = 1 << 22
+    pool = pbm.Pool(T, 64)
+    words = orc.empty_bitmap(T)
+    n = 32 * 8
+    arena = torch.full((n,), -1, dtype=torch.int32, device="cuda")
+    tab = _descs([n], pbm.OP_ALLOC)
+    pool.batch(cfg, None, torch.from_numpy(tab.view(np.uint8).copy()), 1, arena, n, 33, pbm.LAUNCH_PERSISTENT)
+    exp, _ = orc.replay_alloc(words, T, pbm.COLLAB_RW_BM, n, 33)
+    got = arena.cpu().numpy()
+    for c in range(0, n, 32):
+        assert set(got[c:c + 32]) == set(exp[c:c + 32])
+    assert np.array_equal(pool.read_bitmap(), words)
+    pool.close()
+    # mixed swap/free batch of 256 groups at 90%, results into pinned host memory
+    T, occ, seed = 1 << 20, 0.9, 2
+    pool = pbm.Pool(T, 64)
+    pool.prefill(occ, seed)
+    _, held = _held_arena(orc, T, occ, seed)
+    H = len(held)
+    arena = torch.from_numpy(held).cuda()
+    rng = np.random.default_rng(12)
+    counts = rng.integers(1, 300, pbm.MAX_INLINE_GROUPS)
+    ops = [pbm.OP_FREE if i % 7 == 3 else pbm.OP_SWAP for i in range(len(counts))]
+    tab = _descs(counts, ops)
+    h_tab = torch.from_numpy(tab.view(np.uint8).copy()).pin_memory()
+    N = int(counts.sum())
+    res = torch.full((N,), -9, dtype=torch.int32).pin_memory()
+    before = arena.cpu().numpy().copy()
+    bm0 = pool.read_bitmap()
+    for c2 in (pbm.walk_config(pbm.COLLAB_RW_BM, collab_width=64, blocks_per_sm=5), cfg):
+        arena.copy_(torch.from_numpy(before))
+        pool.write_bitmap(bm0)
+        pool.batch(c2, None, h_tab, len(counts), arena, H, 78, pbm.LAUNCH_PERSISTENT, results=res)
+        torch.cuda.synchronize()
+        after = arena.cpu().numpy()
+        r = res.numpy()
+        q = 0
+        for c, op in zip(counts, ops):
+            c = int(c)
+            want = before[q:q + c] if op == pbm.OP_FREE else after[q:q + c]
+            assert np.array_equal(r[q:q + c], want)
+            q += c
+        swapped = np.concatenate([after[int(tab[i]["offset"]):int(tab[i]["offset"]) + int(counts[i])]
+                                  for i in range(len(counts)) if ops[i] == pbm.OP_SWAP])
+        untouched = after[N:]
+        live = np.concatenate([swapped, untouched])
+        assert len(np.unique(live)) == len(live)
+        bits = np.unpackbits(pool.read_bitmap().view(np.uint8), bitorder="little")[:T]
+        want_bits = np.zeros(T, dtype=np.uint8)
+        want_bits[live] = 1
+        assert np.array_equal(bits, want_bits)
+    # too many groups, or a bad op, cannot be carried inline
+    big = _descs([1] * (pbm.MAX_INLINE_GROUPS + 1), pbm.OP_SWAP)
+    with pytest.raises(pbm.PbmError) as e:
+        pool.batch(cfg, None, torch.from_numpy(big.view(np.uint8).copy()), len(big), arena, H, 1,
+                   pbm.LAUNCH_PERSISTENT)
+    assert e.value.rc == pbm.ERR_INVALID
+    bad = _descs([4, 4], [pbm.OP_SWAP, 9])
+    with pytest.raises(pbm.PbmError) as e:
+        pool.batch(cfg, None, torch.from_numpy(bad.view(np.uint8).copy()), 2, arena, H, 1, pbm.LAUNCH_PERSISTENT)
+    assert e.value.rc == pbm.ERR_INVALID
+    pool.close()

@@ -221,7 +221,9 @@ int pbm_batch_launch(pbm_pool *pool, const pbm_walk_config *cfg, const pbm_group
  * found), the page a FREE released.  `results` may be host memory mapped into
  * the device (pinned, e.g. cudaHostAlloc): the kernel then streams the step's
  * results to the host over the chip-to-chip link while it runs, with no
- * separate device-to-host copy.  (No reference counterpart.) */
+ * separate device-to-host copy.  Pageable (unregistered) host memory is
+ * refused with PBM_ERR_INVALID before anything is launched.  (No reference
+ * counterpart.) */
 int pbm_batch_launch_results(pbm_pool *pool, const pbm_walk_config *cfg, const pbm_group *d_groups,
                              const pbm_group *h_groups, uint32_t n_groups, int32_t *d_arena, uint64_t arena_len,
                              uint32_t seed, int32_t *d_steps, int32_t *results, int mode, void *stream);

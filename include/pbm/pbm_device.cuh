@@ -217,18 +217,24 @@ __device__ __forceinline__ int32_t walk_word(const PoolView& v, int32_t seed0,
 // ---------------------------------------------------------------------------
 // Warp-collaborative walk (CollabRW_BM, source/CollabRW_BM.cuh:114-160,
 // restated lock-free).  A group of W lanes (W = 8, 16 or 32, aligned within
-// the warp) shares one LCG stream.  Per jump lane i reads word
-// (base + i*stride) mod L with one coalesced load when stride == 1; the
-// group claims exactly as many clear bits as it still needs -- lowest lanes
-// and lowest bits first, one atomicOr per word -- and hands the bits it
-// gained to the needing lanes in lane order (needing lane of rank r takes
-// the r-th gained bit).  Nothing is over-claimed, so nothing is written back.
-// Needs left unmet (too few free bits, or bits a concurrent claim took
-// first) go to the next jump.  (Planning once more in the same words from the
-// values the atomics returned saved few jumps and cost more instructions
-// than it saved on GB300, so a lost bit simply waits for the next jump.)
-// Lanes whose words coincide
-// (only possible when W*stride > L) are de-duplicated with __match_any_sync.
+// the warp) shares one LCG stream.  Per jump lane i takes word
+// (base + i*stride) mod L -- one cache line for the group when stride == 1 --
+// with one atomicOr of all ones: the read and the claim of every clear bit
+// of the word in a single round trip, as the reference grabs whole words.
+// The group keeps as many of those bits as it still needs -- lowest lanes
+// and lowest bits first -- and hands the rest straight back with one
+// atomicAnd per word (the reference writes whole words back with atomicExch,
+// which drops pages freed meanwhile; an AND of exactly the surplus cannot).
+// The kept bits go to the needing lanes in lane order (needing lane of rank
+// r takes the r-th kept bit).  Needs left unmet go to the next jump.  Every
+// bit a lane takes is its own, so no claim is ever lost to a concurrent one;
+// surplus bits are held only between the two atomics, and a walker that
+// reads them in that window skips them.  (Reading the words first and then
+// claiming only the planned bits costs a second dependent round trip per
+// jump; on GB300 the single grab is 5-7% faster at 90% occupancy.)
+// Lanes whose words coincide (only possible when W*stride > L): only the
+// lowest of them grabs (__match_any_sync), so every word is taken once and
+// the result is that of lane order.
 //
 // Every lane of the group must call this converged; `need` says whether the
 // lane requests a page.  All lanes of the group report the same step count
@@ -275,30 +281,20 @@ __device__ __forceinline__ int32_t walk_collab(const PoolView& v, bool need, int
         x = lcg31(x);
         uint32_t w = idx_hi(x, L) + lane_off;
         if (w >= L) w -= L;
-        Word fr = (Word)~load_word(words + w);
-        if (dedupe) {
-            uint32_t peers = __match_any_sync(gmask, w);
-            if ((peers & lt) != 0u) fr = 0;                          // a lower lane reads this word
-        }
+        bool grab = true;
+        if (dedupe) grab = (__match_any_sync(gmask, w) & lt) == 0u;   // a lower lane takes this word
+        const Word fr = grab ? (Word)~atomic_or(words + w, T::full()) : (Word)0;
         {
             const int cnt = popc_w(fr);
             const int incl = group_incl_scan<W>(cnt, gl, gmask);
             const int n = __popc(needm);
-            const Word m = low_bits(fr, n - (incl - cnt));
-            Word got = 0;
-            if (m) got = m & (Word)~atomic_or(words + w, m);
-            const bool lost = __ballot_sync(gmask, got != m) != 0u;
+            const Word got = low_bits(fr, n - (incl - cnt));        // kept: the first n in lane order
+            const Word extra = fr & (Word)~got;
+            if (extra) atomic_and_noret(words + w, (Word)~extra);   // surplus handed back
             const int g = popc_w(got);
-            // inclusive prefix of the bits gained, and their total
-            int gincl, G;
-            if (!lost) {
-                // every planned bit stuck: the gains are the capped free-bit prefix
-                gincl = min(incl, n);
-                G = min(__shfl_sync(gmask, incl, W - 1, W), n);
-            } else {
-                gincl = group_incl_scan<W>(g, gl, gmask);
-                G = __shfl_sync(gmask, gincl, W - 1, W);
-            }
+            // inclusive prefix of the kept bits, and their total
+            const int gincl = min(incl, n);
+            const int G = min(__shfl_sync(gmask, incl, W - 1, W), n);
             if (G > 0) {
                 // needing lane of rank r takes gained bit r: its source is the
                 // first group lane whose inclusive gain exceeds r
@@ -378,28 +374,19 @@ __device__ __forceinline__ void walk_collab2(const PoolView& v, bool need_a, boo
         x = lcg31(x);
         uint32_t w = idx_hi(x, L) + lane_off;
         if (w >= L) w -= L;
-        Word fr = (Word)~load_word(words + w);
-        if (dedupe) {
-            const uint32_t peers = __match_any_sync(kFull32, w);
-            if ((peers & lt) != 0u) fr = 0;                          // a lower lane reads this word
-        }
+        bool grab = true;
+        if (dedupe) grab = (__match_any_sync(kFull32, w) & lt) == 0u;   // a lower lane takes this word
+        const Word fr = grab ? (Word)~atomic_or(words + w, T::full()) : (Word)0;
         const int cnt = popc_w(fr);
         const int incl = group_incl_scan<32>(cnt, lane, kFull32);
         const int na = __popc(ma);
         const int n = na + __popc(mb);
-        const Word m = low_bits(fr, n - (incl - cnt));
-        Word got = 0;
-        if (m) got = m & (Word)~atomic_or(words + w, m);
-        const bool lost = __ballot_sync(kFull32, got != m) != 0u;
+        const Word got = low_bits(fr, n - (incl - cnt));
+        const Word extra = fr & (Word)~got;
+        if (extra) atomic_and_noret(words + w, (Word)~extra);
         const int g = popc_w(got);
-        int gincl, G;
-        if (!lost) {
-            gincl = min(incl, n);
-            G = min(__shfl_sync(kFull32, incl, 31), n);
-        } else {
-            gincl = group_incl_scan<32>(g, lane, kFull32);
-            G = __shfl_sync(kFull32, gincl, 31);
-        }
+        const int gincl = min(incl, n);
+        const int G = min(__shfl_sync(kFull32, incl, 31), n);
         if (G > 0) {
             const bool wa = need_a && id_a < 0, wb = need_b && id_b < 0;
             const int ra = wa ? __popc(ma & lt) : 0;
@@ -419,9 +406,10 @@ __device__ __forceinline__ void walk_collab2(const PoolView& v, bool need_a, boo
 // ---------------------------------------------------------------------------
 // The collaborative walk over an arbitrary set of converged lanes `active`
 // (the drop-in form: the reference's getPage runs on __activemask(),
-// CollabRW_BM.cuh:119).  Active lane k (k-th set bit of `active`) reads word
-// (base + k) mod L; prefix sums use bit-sliced ballots, so inactive lanes
-// never participate.  `slots` = 32 ints of shared memory for this warp.
+// CollabRW_BM.cuh:119).  Active lane k (k-th set bit of `active`) takes word
+// (base + k) mod L with the same grab and hand-back as walk_collab; prefix
+// sums use bit-sliced ballots, so inactive lanes never participate.  `slots`
+// = 32 ints of shared memory for this warp.
 // ---------------------------------------------------------------------------
 template <typename Word>
 __device__ __forceinline__ int32_t walk_collab_masked(const PoolView& v, uint32_t active, bool need,
@@ -444,23 +432,17 @@ __device__ __forceinline__ int32_t walk_collab_masked(const PoolView& v, uint32_
         x = lcg31(x);
         uint32_t w = idx_hi(x, L) + off;
         if (w >= L) w -= L;
-        Word val = load_word(words + w);
-        if (dedupe) {
-            uint32_t peers = __match_any_sync(active, w);
-            if ((peers & lt) != 0u) val = T::full();
-        }
-        Word fr = (Word)~val;
+        bool grab = true;
+        if (dedupe) grab = (__match_any_sync(active, w) & lt) == 0u;   // a lower lane takes this word
+        const Word fr = grab ? (Word)~atomic_or(words + w, T::full()) : (Word)0;
         int cnt = popc_w(fr);
         int pre = 0;
 #pragma unroll
         for (int b = 0; b < 7; ++b) pre += __popc(__ballot_sync(active, (cnt >> b) & 1) & lt) << b;
         int n = __popc(needm);
-        Word m = low_bits(fr, n - pre);
-        Word got = 0;
-        if (m) {
-            Word old = atomic_or(words + w, m);
-            got = m & (Word)~old;
-        }
+        Word got = low_bits(fr, n - pre);                            // kept; the surplus goes back
+        const Word extra = fr & (Word)~got;
+        if (extra) atomic_and_noret(words + w, (Word)~extra);
         int g = popc_w(got);
         int gpre = 0, G = 0;
 #pragma unroll

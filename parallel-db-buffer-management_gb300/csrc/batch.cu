@@ -437,6 +437,7 @@ int pbm_batch_launch_results(pbm_pool* pool, const pbm_walk_config* cfg, const p
     if (!pool || !d_arena || arena_len == 0) return PBM_ERR_INVALID;
     int rc = valid_cfg(cfg);
     if (rc) return rc;
+    if (results && !device_writable(results)) return PBM_ERR_INVALID;
     if (n_groups == 0) return PBM_OK;
     cudaStream_t s = (cudaStream_t)stream;
     pool->fifo_valid = false;
@@ -514,6 +515,7 @@ int pbm_batch_graph_create_results(pbm_pool* pool, const pbm_walk_config* cfg, c
                                    uint32_t seed0, int32_t* results, void* stream, pbm_graph** out) {
     if (!pool || !d_groups || !d_arena || !out || n_groups == 0 || n_steps == 0 || arena_len == 0)
         return PBM_ERR_INVALID;
+    if (results && !device_writable(results)) return PBM_ERR_INVALID;
     int rc = valid_cfg(cfg);
     if (rc) return rc;
     *out = nullptr;

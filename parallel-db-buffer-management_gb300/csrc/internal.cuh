@@ -19,6 +19,7 @@ extern std::atomic<unsigned long long> g_launches;
 inline void count_launch(unsigned long long n = 1) { g_launches.fetch_add(n, std::memory_order_relaxed); }
 
 int sm_count();
+bool device_writable(const void* p);
 
 constexpr uint32_t kDefaultMaxSteps = 4096;
 

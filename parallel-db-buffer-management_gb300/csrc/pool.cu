@@ -26,6 +26,20 @@ int sm_count() {
     return cached;
 }
 
+// Whether a kernel may write p: device or managed memory, or host memory that
+// is pinned and mapped (cudaHostAlloc, cudaHostRegister).  Plain pageable host
+// memory is refused, so a wrong buffer is an error status and never a kernel
+// touching an unmapped address.
+bool device_writable(const void* p) {
+    cudaPointerAttributes at{};
+    if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    if (at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged) return true;
+    return at.type == cudaMemoryTypeHost && at.devicePointer == p;
+}
+
 // Bernoulli(occ) bitmap: one thread per 32-bit word, one hash per page.
 __global__ void k_prefill(uint32_t* words, uint32_t n_words, uint64_t n_pages,
                           uint64_t thresh53, uint64_t seed) {

@@ -319,3 +319,26 @@ def test_inline_table_launch(cuda, pbm_mod, orc):
         pool.batch(cfg, None, torch.from_numpy(bad.view(np.uint8).copy()), 2, arena, H, 1, pbm.LAUNCH_PERSISTENT)
     assert e.value.rc == pbm.ERR_INVALID
     pool.close()
+
+
+def test_results_buffer_must_be_device_writable(cuda, pbm_mod, orc):
+    """A pageable host buffer for results is refused before any launch (the
+    kernel would otherwise write an address the device cannot reach)."""
+    torch = cuda
+    pbm = pbm_mod
+    T = 1 << 16
+    pool = pbm.Pool(T, 64)
+    arena = torch.full((64,), -1, dtype=torch.int32, device="cuda")
+    tab = _descs([64], pbm.OP_ALLOC)
+    d_tab = torch.from_numpy(tab.view(np.uint8).copy()).cuda()
+    pageable = np.full(64, -9, dtype=np.int32)
+    cfg = pbm.walk_config(pbm.COLLAB_RW_BM)
+    with pytest.raises(pbm.PbmError) as e:
+        pool.batch(cfg, d_tab, None, 1, arena, 64, 1, pbm.LAUNCH_PERSISTENT, results=pageable.ctypes.data)
+    assert e.value.rc == pbm.ERR_INVALID
+    with pytest.raises(pbm.PbmError) as e:
+        pool.graph(cfg, d_tab, 1, 1, arena, 64, 1, results=pageable.ctypes.data)
+    assert e.value.rc == pbm.ERR_INVALID
+    torch.cuda.synchronize()
+    assert pool.used() == 0 and (pageable == -9).all()
+    pool.close()

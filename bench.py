@@ -60,7 +60,7 @@ UNIT = "ops/s"
 # dram__bytes_write.sum of one captured launch (7.82 MB for the 1,420,753-pair
 # step of `bench.py --profile --profile-walk pair32c`), summarised in
 # profiles/batch_persistent_collab32_90pct.md.
-NCU_DRAM_BYTES_PER_PAIR = 7.817984e6 / 1420753
+NCU_DRAM_BYTES_PER_PAIR = 7.815424e6 / 1420753
 
 
 def env_rank():

@@ -67,28 +67,68 @@ struct BmView {
 // hand moves one position per atomic, as the reference's SingleClock arm.
 constexpr uint32_t kHandBatch = 1;
 
+// Per-slot hand (DistClock, parallelPage.cu:571-592): the slot's hand is
+// private, so it reads the next kLookahead frames' words and reference bits
+// in one round trip and then examines them in hand order exactly as the
+// one-step sweep does, stopping at the victim (the hand ends just past it,
+// and frames beyond it are untouched).  Never more frames at once than the
+// pool has, so one batch never sees a frame twice.
+constexpr uint32_t kLookahead = 8;
+
+__device__ __forceinline__ int32_t sweep_private(const BmView& b, uint32_t page, uint32_t slot,
+                                                 uint32_t* old_page) {
+    uint32_t arm = b.arms[slot];
+    if (arm >= b.n_frames) arm %= b.n_frames;
+    const uint32_t width = b.n_frames < kLookahead ? b.n_frames : kLookahead;
+    int32_t out = -1;
+    for (uint32_t done = 0; done < b.max_sweep && out < 0;) {
+        unsigned long long st[kLookahead];
+        uint8_t rf[kLookahead];
+#pragma unroll
+        for (uint32_t j = 0; j < kLookahead; ++j) {
+            if (j < width) {
+                uint32_t f = arm + j;
+                if (f >= b.n_frames) f -= b.n_frames;
+                st[j] = __ldcg(b.frame_state + f);
+                rf[j] = b.ref[f];
+            }
+        }
+#pragma unroll
+        for (uint32_t j = 0; j < kLookahead; ++j) {
+            if (j >= width || done >= b.max_sweep || out >= 0) break;
+            const uint32_t f = arm;
+            arm = f + 1u == b.n_frames ? 0u : f + 1u;
+            ++done;
+            if ((uint32_t)st[j] != 0u) continue;                // pinned
+            if (rf[j]) { b.ref[f] = 0; continue; }              // second chance
+            const unsigned long long ns = ((unsigned long long)page << 32) | 1ull;
+            if (atomicCAS(b.frame_state + f, st[j], ns) == st[j]) {
+                *old_page = (uint32_t)(st[j] >> 32);
+                out = (int32_t)f;
+            }
+        }
+    }
+    b.arms[slot] = arm;
+    return out;
+}
+
 // Victim search; returns a frame now holding (page, 1 pin) and its old page.
 // The shared hand advances `batch` positions per atomic, which the sweeping
 // thread then examines in order (parallelPage.cu:491-509 steps it by one).
+template <bool DIST>
 __device__ __forceinline__ int32_t sweep(const BmView& b, uint32_t page, uint32_t slot, uint32_t batch,
                                          uint32_t* old_page) {
-    uint32_t arm = b.dist ? b.arms[slot] : 0u;
+    if constexpr (DIST) return sweep_private(b, page, slot, old_page);
     unsigned long long res = 0;
     uint32_t res_left = 0;
     int32_t out = -1;
     for (uint32_t i = 0; i < b.max_sweep; ++i) {
-        uint32_t f;
-        if (b.dist) {
-            f = arm >= b.n_frames ? arm - b.n_frames : arm;
-            arm = f + 1u;
-        } else {
-            if (res_left == 0u) {
-                res = atomicAdd(b.single_hand, (unsigned long long)batch);
-                res_left = batch;
-            }
-            f = (uint32_t)((res + (batch - res_left)) % b.n_frames);
-            --res_left;
+        if (res_left == 0u) {
+            res = atomicAdd(b.single_hand, (unsigned long long)batch);
+            res_left = batch;
         }
+        const uint32_t f = (uint32_t)((res + (batch - res_left)) % b.n_frames);
+        --res_left;
         unsigned long long s = __ldcg(b.frame_state + f);
         if ((uint32_t)s != 0u) continue;                    // pinned
         if (b.ref[f]) { b.ref[f] = 0; continue; }           // second chance
@@ -99,7 +139,6 @@ __device__ __forceinline__ int32_t sweep(const BmView& b, uint32_t page, uint32_
             break;
         }
     }
-    if (b.dist) b.arms[slot] = arm;
     return out;
 }
 
@@ -116,6 +155,7 @@ __device__ __forceinline__ bool pin_if_owner(const BmView& b, int32_t f, uint32_
     return false;
 }
 
+template <bool DIST>
 __device__ __forceinline__ int32_t fetch(const BmView& b, uint32_t page, uint32_t slot, uint32_t batch, BmAcc& acc) {
     for (uint32_t attempt = 0; attempt < kFetchSpinLimit; ++attempt) {
         int32_t f = __ldcg(b.page_table + page);
@@ -130,7 +170,7 @@ __device__ __forceinline__ int32_t fetch(const BmView& b, uint32_t page, uint32_
         if (f == -1) {
             if (atomicCAS(b.page_table + page, -1, kLoading) != -1) continue;
             uint32_t old_page = kEmptyPage;
-            int32_t h = sweep(b, page, slot, batch, &old_page);
+            int32_t h = sweep<DIST>(b, page, slot, batch, &old_page);
             if (h < 0) {
                 atomicExch(b.page_table + page, -1);
                 ++acc.failures;
@@ -157,6 +197,101 @@ __device__ __forceinline__ int32_t fetch(const BmView& b, uint32_t page, uint32_
     return -1;
 }
 
+// Warp-cooperative CLOCK sweep on the single hand.  The lanes in `loaders`
+// (each the loader of its own `page`, its page-table entry already set to
+// loading) need victim frames.  Per batch the warp takes 32 consecutive hand
+// positions with one atomicAdd and every lane examines one frame, as the
+// one-thread sweep does: a pinned frame is passed, a referenced one loses its
+// reference bit (second chance), an unpinned unreferenced one is a candidate.
+// Candidates go in hand order to the loaders in lane order, each taken with
+// the one-thread sweep's CAS (a pin that arrived in between makes it fail and
+// the loader waits for the next batch); candidates beyond the loaders' need
+// are passed.  A loader gives up after its max_sweep positions.  So a miss
+// costs about one batch of round trips instead of one per frame examined.
+// The whole warp calls converged; returns the lane's frame (-1 if none) and
+// the page it held.
+__device__ __forceinline__ int32_t sweep_warp(const BmView& b, uint32_t loaders, uint32_t page,
+                                              uint32_t* old_page) {
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t lt = (1u << lane) - 1u;
+    int32_t out = -1;
+    const uint32_t max_batches = b.max_sweep > 32u ? (b.max_sweep + 31u) / 32u : 1u;
+    for (uint32_t it = 0; loaders != 0u && it < max_batches; ++it) {
+        unsigned long long base = 0;
+        if (lane == 0u) base = atomicAdd(b.single_hand, 32ull);
+        base = __shfl_sync(0xffffffffu, base, 0);
+        const uint32_t f = (uint32_t)((base + lane) % b.n_frames);
+        const unsigned long long st = __ldcg(b.frame_state + f);
+        bool cand = false;
+        if ((uint32_t)st == 0u) {                   // unpinned
+            if (b.ref[f]) b.ref[f] = 0;             // second chance
+            else cand = true;
+        }
+        const uint32_t cm = __ballot_sync(0xffffffffu, cand);
+        const int n_load = __popc(loaders);
+        // candidate of rank k serves the loader of rank k
+        const int k = __popc(cm & lt);
+        const int target = (cand && k < n_load) ? (int)__fns(loaders, 0u, k + 1) : -1;
+        const uint32_t tpage = __shfl_sync(0xffffffffu, page, target < 0 ? (int)lane : target);
+        bool took = false;
+        if (target >= 0) {
+            const unsigned long long ns = ((unsigned long long)tpage << 32) | 1ull;
+            took = atomicCAS(b.frame_state + f, st, ns) == st;
+        }
+        const uint32_t tm = __ballot_sync(0xffffffffu, took);
+        const bool is_loader = (loaders >> lane) & 1u;
+        const int r = __popc(loaders & lt);
+        const int src = (is_loader && r < __popc(cm)) ? (int)__fns(cm, 0u, r + 1) : -1;
+        const uint32_t got_f = __shfl_sync(0xffffffffu, f, src < 0 ? (int)lane : src);
+        const unsigned long long got_s = __shfl_sync(0xffffffffu, st, src < 0 ? (int)lane : src);
+        if (src >= 0 && ((tm >> src) & 1u)) {
+            out = (int32_t)got_f;
+            *old_page = (uint32_t)(got_s >> 32);
+        }
+        loaders = __ballot_sync(0xffffffffu, is_loader && out < 0);
+    }
+    return out;
+}
+
+// The loaders' side of a cooperative miss: unmap the victims' old pages, copy
+// each new page from the backing store with the whole warp (one loader at a
+// time, 16 bytes per lane per step), then publish the page-table entries.
+// The whole warp calls converged; h = the lane's frame from sweep_warp.
+__device__ __forceinline__ void finish_loads_warp(const BmView& b, bool loader, uint32_t page, int32_t h,
+                                                  uint32_t old_page, BmAcc& acc) {
+    if (loader) {
+        if (h < 0) {
+            atomicExch(b.page_table + page, -1);
+            ++acc.failures;
+        } else if (old_page != kEmptyPage) {
+            atomicExch(b.page_table + old_page, -1);
+            ++acc.evictions;
+        }
+    }
+    if (b.backing && b.frames) {
+        const uint32_t lane = threadIdx.x & 31u;
+        const uint32_t n16 = b.frame_size / 16u;
+        uint32_t todo = __ballot_sync(0xffffffffu, loader && h >= 0);
+        while (todo) {
+            const int l = __ffs((int)todo) - 1;
+            todo &= todo - 1u;
+            const uint32_t pg = __shfl_sync(0xffffffffu, page, l);
+            const int32_t fr = __shfl_sync(0xffffffffu, h, l);
+            const int4* src = reinterpret_cast<const int4*>(b.backing + (size_t)pg * b.frame_size);
+            int4* dst = reinterpret_cast<int4*>(b.frames + (size_t)fr * b.frame_size);
+            for (uint32_t k = lane; k < n16; k += 32u) dst[k] = src[k];
+        }
+        __threadfence();
+        __syncwarp();
+    }
+    if (loader && h >= 0) {
+        b.ref[h] = 1;
+        __threadfence();
+        atomicExch(b.page_table + page, h);
+        ++acc.misses;
+    }
+}
+
 // Releases k pins of frame f with one atomic.  A release of more pins than
 // the frame holds (a caller error) is taken back and counted as bad; its
 // subtraction can borrow from the page field for that instant, which makes a
@@ -175,6 +310,8 @@ __device__ __forceinline__ void unpin_k(const BmView& b, int32_t f, uint32_t k, 
 
 // One round: release the listed pins, then fetch this round's pages.
 // With one thread this is the deterministic replay of the round.
+// DIST: per-slot hands (b.dist), else the single shared hand.
+template <bool DIST>
 __global__ void __launch_bounds__(256) k_round(BmView b, const int32_t* release_frames_of,
                                                const int32_t* release_idx, uint32_t n_release,
                                                const int32_t* pages, uint32_t n, uint32_t slot0,
@@ -202,7 +339,7 @@ __global__ void __launch_bounds__(256) k_round(BmView b, const int32_t* release_
         for (uint32_t i = 0; i < n; ++i) {
             int32_t p = pages[i];
             int32_t f = -1;
-            if (p >= 0 && (uint32_t)p < b.n_logical) f = fetch(b, (uint32_t)p, (slot0 + i) % b.n_arms, 1u, acc);
+            if (p >= 0 && (uint32_t)p < b.n_logical) f = fetch<DIST>(b, (uint32_t)p, (slot0 + i) % b.n_arms, 1u, acc);
             frames_out[i] = f;
         }
     } else {
@@ -216,9 +353,9 @@ __global__ void __launch_bounds__(256) k_round(BmView b, const int32_t* release_
             const uint32_t key = valid ? (uint32_t)p : 0x80000000u + lane;   // invalid lanes never merge
             const uint32_t peers = __match_any_sync(0xffffffffu, key);
             const uint32_t leader = (uint32_t)__ffs((int)peers) - 1u;
-            int32_t hit = -1;
+            int32_t hit = -1, f0 = kLoading;
             if (valid && lane == leader) {
-                const int32_t f0 = __ldcg(b.page_table + p);
+                f0 = __ldcg(b.page_table + p);
                 if (f0 >= 0 && pin_if_owner(b, f0, (uint32_t)p, (uint32_t)__popc(peers))) {
                     b.ref[f0] = 1;
                     hit = f0;
@@ -226,11 +363,26 @@ __global__ void __launch_bounds__(256) k_round(BmView b, const int32_t* release_
             }
             hit = __shfl_sync(0xffffffffu, hit, (int)leader);
             int32_t f = -1;
+            bool loader = false;
+            if constexpr (!DIST) {
+                // single hand: the leaders of pages that are not resident become
+                // their loaders and sweep together; the other lanes fetch as below
+                // (their pages are resident, or being loaded, by then)
+                if (hit < 0 && valid && lane == leader)
+                    loader = f0 == -1 && atomicCAS(b.page_table + p, -1, kLoading) == -1;
+                const uint32_t lm = __ballot_sync(0xffffffffu, loader);
+                if (lm) {
+                    uint32_t old_page = kEmptyPage;
+                    const int32_t h = sweep_warp(b, lm, (uint32_t)p, &old_page);
+                    finish_loads_warp(b, loader, (uint32_t)p, h, old_page, acc);
+                    if (loader) f = h;
+                }
+            }
             if (hit >= 0) {
                 f = hit;
                 ++acc.hits;
-            } else if (valid) {
-                f = fetch(b, (uint32_t)p, (slot0 + i) % b.n_arms, kHandBatch, acc);
+            } else if (valid && !loader) {
+                f = fetch<DIST>(b, (uint32_t)p, (slot0 + i) % b.n_arms, kHandBatch, acc);
             }
             if (i < n) frames_out[i] = f;
         }
@@ -381,8 +533,12 @@ int pbm_bufmgr_round(pbm_bufmgr* m, const int32_t* d_frames_of, const int32_t* d
     const uint32_t work = n > n_release ? n : n_release;
     int block = serial ? 1 : 256;
     int grid = serial ? 1 : (int)((work + 255u) / 256u);
-    k_round<<<grid, block, 0, (cudaStream_t)stream>>>(m->v, d_frames_of, d_release_idx, n_release, d_pages,
-                                                       n, slot0, d_frames_out);
+    if (m->v.dist)
+        k_round<true><<<grid, block, 0, (cudaStream_t)stream>>>(m->v, d_frames_of, d_release_idx, n_release,
+                                                                d_pages, n, slot0, d_frames_out);
+    else
+        k_round<false><<<grid, block, 0, (cudaStream_t)stream>>>(m->v, d_frames_of, d_release_idx, n_release,
+                                                                 d_pages, n, slot0, d_frames_out);
     PBM_LAUNCH_CHECK();
     return PBM_OK;
 }

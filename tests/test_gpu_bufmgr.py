@@ -87,3 +87,34 @@ def test_parallel_rounds_invariants_and_copy(cuda, pbm_mod, policy, n_arms):
     assert ok.mean() > 0.99
     assert np.array_equal(got[ok], lp[ok])
     bm.close()
+
+
+@pytest.mark.parametrize("policy,n_arms", [(0, 1), (1, 8)])
+def test_parallel_rounds_fewer_frames_than_a_warp(cuda, pbm_mod, policy, n_arms):
+    """16 frames, so one warp's sweep batch wraps the frames twice (two lanes
+    examine each frame) and most fetches find every frame pinned: fetches
+    fail after their bounded sweep, and the maps stay consistent."""
+    torch = cuda
+    pbm = pbm_mod
+    n_logical, n_frames, rounds, R = 256, 16, 12, 256
+    pages, ptr, idx = _trace(n_logical, rounds, R, 8)
+    bm = pbm.BufferManager(n_logical, n_frames, policy=policy, n_arms=n_arms)
+    d_pages = torch.from_numpy(pages).cuda()
+    d_idx = torch.from_numpy(idx).cuda()
+    d_frames = torch.full((rounds * R,), -1, dtype=torch.int32, device="cuda")
+    released = np.zeros(rounds * R, dtype=bool)
+    for r in range(rounds):
+        a, b = int(ptr[r]), int(ptr[r + 1])
+        bm.round(d_frames, d_idx[a:] if b > a else None, b - a, d_pages[r * R:], R, r * R, d_frames[r * R:])
+        released[idx[a:b]] = True
+        chk = bm.check()
+        assert chk.mismatches == 0 and chk.loading == 0 and chk.resident == chk.mapped_frames
+        fr = d_frames[:(r + 1) * R].cpu().numpy()
+        assert ((fr >= -1) & (fr < n_frames)).all()
+        held = (~released[:(r + 1) * R]) & (fr >= 0)
+        assert chk.pins == int(held.sum())
+    c = bm.counters()
+    assert c.bad_unpins == 0 and c.timeouts == 0
+    assert c.hits + c.misses + c.failures == rounds * R
+    assert c.failures > 0 and c.misses > 0
+    bm.close()

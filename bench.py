@@ -818,7 +818,8 @@ def run_configs(args, torch, pbm, stream):
 def run_profile_kernel(args):
     """Small, bounded cases of the other kernels for ncu captures (a few GB
     on the device at most, inputs larger than L2 where the kernel reads
-    any): `bufmgr` 16 rounds of 2^18 Zipf fetches on 2^22 frames (k_round),
+    any): `bufmgr` 16 rounds of 2^18 Zipf fetches on 2^20 frames, full and
+    evicting from round 11 on (k_round),
     `malloc` 8 rounds of 32 malloc groups + frees on a 2 GiB pool
     (k_malloc_persistent), `alloc` 2^22 collaborative claims at 50%
     (k_alloc_collab) followed by `free` of half of them (k_free_pages)."""
@@ -838,15 +839,20 @@ def run_profile_kernel(args):
         d_pages = torch.from_numpy(pages).cuda()
         d_idx = torch.from_numpy(idx).cuda()
         d_frames = torch.full((R * rounds,), -1, dtype=torch.int32, device="cuda")
-        bm = pbm.BufferManager(1 << 24, 1 << 22, policy=pbm.BM_SINGLE_CLOCK)
+        bm = pbm.BufferManager(1 << 24, 1 << 20, policy=pbm.BM_SINGLE_CLOCK)
+        per_round = []
         for r in range(rounds):
             a, b = int(ptr[r]), int(ptr[r + 1])
             flush.zero_()
             bm.round(d_frames, d_idx[a:] if b > a else None, b - a, d_pages[r * R:], R, r * R, d_frames[r * R:],
                      stream=sh)
+            c = bm.counters(sh)
+            per_round.append((c.hits, c.misses, c.evictions))
         torch.cuda.synchronize()
         c = bm.counters(sh)
-        out.update(hits=c.hits, misses=c.misses, mismatches=bm.check(sh).mismatches)
+        d = np.diff(np.array([(0, 0, 0)] + per_round), axis=0)
+        out.update(hits=c.hits, misses=c.misses, mismatches=bm.check(sh).mismatches,
+                   per_round_hits_misses_evictions=d.tolist())
         bm.close()
     elif args.profile_kernel == "malloc":
         T, groups, rounds = 1 << 19, 32, 8

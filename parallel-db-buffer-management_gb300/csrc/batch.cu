@@ -14,6 +14,7 @@
 //               block to finish advances the device-resident step counter, so
 //               each replay is one launch that reads the next step's
 //               descriptors from device memory.
+#include <atomic>
 #include <type_traits>
 
 #include "batch_common.cuh"
@@ -287,21 +288,23 @@ using namespace pbm;
 namespace {
 
 // Resident blocks per SM of a persistent instantiation (queried once per block
-// size, outside any stream capture).
+// size, outside any stream capture).  The cache is one atomic word, (block
+// size << 16) | blocks, so host threads launching batches at once never read
+// a block size paired with another size's count.
 template <BWalk K, int W, typename Word, int MINB, typename Tab = NoTable>
 int persistent_blocks_per_sm(int block) {
-    static int cached_block = 0, cached = 0;
-    if (cached_block != block) {
-        int n = 0;
-        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_batch_persistent<K, W, Word, MINB, Tab>, block, kFusedPrefixBytes) !=
-            cudaSuccess) {
-            cudaGetLastError();
-            n = 1;
-        }
-        cached = n > 0 ? n : 1;
-        cached_block = block;
+    static std::atomic<uint32_t> cache{0u};
+    const uint32_t c = cache.load(std::memory_order_relaxed);
+    if ((int)(c >> 16) == block) return (int)(c & 0xffffu);
+    int n = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_batch_persistent<K, W, Word, MINB, Tab>, block,
+                                                      kFusedPrefixBytes) != cudaSuccess) {
+        cudaGetLastError();
+        n = 1;
     }
-    return cached;
+    n = n > 0 ? (n < 0xffff ? n : 0xffff) : 1;
+    cache.store(((uint32_t)block << 16) | (uint32_t)n, std::memory_order_relaxed);
+    return n;
 }
 
 // blocks_per_sm <= 0: uncapped registers, as many blocks as fit;

@@ -9,6 +9,8 @@
 #include <cstring>
 #include <new>
 
+#include <atomic>
+
 #include "internal.cuh"
 
 namespace pbm {
@@ -16,14 +18,16 @@ namespace pbm {
 std::atomic<unsigned long long> g_launches{0};
 
 int sm_count() {
-    static int cached = 0;
-    if (!cached) {
+    static std::atomic<int> cached{0};
+    int c = cached.load(std::memory_order_relaxed);
+    if (!c) {
         int dev = 0, n = 0;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
-        cached = n > 0 ? n : 1;
+        c = n > 0 ? n : 1;
+        cached.store(c, std::memory_order_relaxed);
     }
-    return cached;
+    return c;
 }
 
 // Whether a kernel may write p: device or managed memory, or host memory that

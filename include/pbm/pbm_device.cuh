@@ -126,12 +126,29 @@ __device__ __forceinline__ int popc_w(uint64_t x) { return __popcll(x); }
 __device__ __forceinline__ int ctz_w(uint32_t x) { return __ffs((int)x) - 1; }
 __device__ __forceinline__ int ctz_w(uint64_t x) { return __ffsll((long long)x) - 1; }
 
+// Position of the (k+1)-th set bit of m (0 <= k < popc(m)): five halving
+// steps, each counting the set bits of the lower half and moving into the
+// upper half when k lies beyond them (branch-free, no loop; measured faster
+// than __fns in the walks).
+__device__ __forceinline__ uint32_t nth_set_bit(uint32_t m, int k) {
+    uint32_t pos = 0;
+    int c = __popc(m & 0xffffu);
+    if (k >= c) { k -= c; pos += 16u; m >>= 16; }
+    c = __popc(m & 0xffu);
+    if (k >= c) { k -= c; pos += 8u; m >>= 8; }
+    c = __popc(m & 0xfu);
+    if (k >= c) { k -= c; pos += 4u; m >>= 4; }
+    c = __popc(m & 0x3u);
+    if (k >= c) { k -= c; pos += 2u; m >>= 2; }
+    if (k >= (int)(m & 1u)) pos += 1u;
+    return pos;
+}
+
 // Lowest k set bits of m (0 <= k <= popc(m)).
 __device__ __forceinline__ uint32_t low_bits(uint32_t m, int k) {
     if (k <= 0) return 0u;
     if (k >= __popc(m)) return m;
-    uint32_t pos = __fns(m, 0u, k + 1);       // position of the (k+1)-th set bit
-    return m & ((1u << pos) - 1u);
+    return m & ((1u << nth_set_bit(m, k)) - 1u);   // below the (k+1)-th set bit
 }
 __device__ __forceinline__ uint64_t low_bits(uint64_t m, int k) {
     if (k <= 0) return 0ull;
@@ -252,11 +269,11 @@ __device__ __forceinline__ int group_incl_scan(int v, uint32_t gl, uint32_t gmas
 }
 
 // Position of the (k+1)-th set bit of m (k < popc(m)).
-__device__ __forceinline__ uint32_t nth_bit(uint32_t m, int k) { return __fns(m, 0u, k + 1); }
+__device__ __forceinline__ uint32_t nth_bit(uint32_t m, int k) { return nth_set_bit(m, k); }
 __device__ __forceinline__ uint32_t nth_bit(uint64_t m, int k) {
     const uint32_t lo = (uint32_t)m;
     const int c = __popc(lo);
-    return k < c ? __fns(lo, 0u, k + 1) : 32u + __fns((uint32_t)(m >> 32), 0u, k - c + 1);
+    return k < c ? nth_set_bit(lo, k) : 32u + nth_set_bit((uint32_t)(m >> 32), k - c);
 }
 
 template <int W, typename Word>

@@ -188,7 +188,7 @@ __device__ __forceinline__ void* qmalloc_group(const QMallocView& q, uint32_t ac
     // the carver of refill lane i is the refill lane (i / b) * b of the same class
     const uint32_t refill_mask = __ballot_sync(active, refill) & peers;
     uint32_t src = lane;
-    if (refill) src = (uint32_t)__fns(refill_mask, 0u, (ri / b) * b + 1u);
+    if (refill) src = nth_set_bit(refill_mask, (int)((ri / b) * b));
     const int32_t base = __shfl_sync(active, chunk, (int)(refill ? src : lane));
     if (refill && base >= 0) {
         const uint32_t bytes = 1u << (kMallocMinShift + cls);

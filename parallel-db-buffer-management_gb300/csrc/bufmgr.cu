@@ -231,7 +231,7 @@ __device__ __forceinline__ int32_t sweep_warp(const BmView& b, uint32_t loaders,
         const int n_load = __popc(loaders);
         // candidate of rank k serves the loader of rank k
         const int k = __popc(cm & lt);
-        const int target = (cand && k < n_load) ? (int)__fns(loaders, 0u, k + 1) : -1;
+        const int target = (cand && k < n_load) ? (int)nth_set_bit(loaders, k) : -1;
         const uint32_t tpage = __shfl_sync(0xffffffffu, page, target < 0 ? (int)lane : target);
         bool took = false;
         if (target >= 0) {
@@ -241,7 +241,7 @@ __device__ __forceinline__ int32_t sweep_warp(const BmView& b, uint32_t loaders,
         const uint32_t tm = __ballot_sync(0xffffffffu, took);
         const bool is_loader = (loaders >> lane) & 1u;
         const int r = __popc(loaders & lt);
-        const int src = (is_loader && r < __popc(cm)) ? (int)__fns(cm, 0u, r + 1) : -1;
+        const int src = (is_loader && r < __popc(cm)) ? (int)nth_set_bit(cm, r) : -1;
         const uint32_t got_f = __shfl_sync(0xffffffffu, f, src < 0 ? (int)lane : src);
         const unsigned long long got_s = __shfl_sync(0xffffffffu, st, src < 0 ? (int)lane : src);
         if (src >= 0 && ((tm >> src) & 1u)) {

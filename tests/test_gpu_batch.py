@@ -342,3 +342,50 @@ def test_results_buffer_must_be_device_writable(cuda, pbm_mod, orc):
     torch.cuda.synchronize()
     assert pool.used() == 0 and (pageable == -9).all()
     pool.close()
+
+
+@pytest.mark.parametrize("mode", ["plain", "persistent", "inline", "graph"])
+def test_empty_groups_and_largest_group(cuda, pbm_mod, orc, mode):
+    """Groups with no requests between others (first, middle, last), a group
+    of the largest size (65,536 requests) and a batch of no groups: every
+    request is served in request order, empty groups take no slot, and the
+    invariants hold in every launch form."""
+    torch = cuda
+    pbm = pbm_mod
+    T, occ, seed = 1 << 20, 0.9, 2
+    pool = pbm.Pool(T, 64)
+    pool.prefill(occ, seed)
+    _, held = _held_arena(orc, T, occ, seed)
+    H = len(held)
+    arena = torch.from_numpy(held).cuda()
+    counts = [0, 65536, 0, 0, 17, 1, 0, 300, 0]
+    tab = _descs(counts, pbm.OP_SWAP)
+    N = sum(counts)
+    res = torch.full((N,), -9, dtype=torch.int32, device="cuda")
+    cfg = pbm.walk_config(pbm.COLLAB_RW_BM, collab_width=64, blocks_per_sm=5)
+    d_tab = torch.from_numpy(tab.view(np.uint8).copy()).cuda()
+    hg = pbm.groups_array([(int(r["op"]), int(r["count"]), int(r["offset"])) for r in tab])
+    # a batch of no groups is a no-op in every form
+    pool.batch(cfg, d_tab, hg, 0, arena, H, 1, pbm.LAUNCH_PERSISTENT)
+    pool.batch(cfg, d_tab, hg, 0, arena, H, 1, pbm.LAUNCH_PLAIN)
+    torch.cuda.synchronize()
+    assert pool.stats().successes == 0
+    if mode == "graph":
+        g = pool.graph(cfg, d_tab, len(counts), 1, arena, H, 41, results=res)
+        g.replay()
+        g.close()
+    elif mode == "inline":
+        pool.batch(cfg, None, torch.from_numpy(tab.view(np.uint8).copy()), len(counts), arena, H, 41,
+                   pbm.LAUNCH_PERSISTENT, results=res)
+    else:
+        pool.batch(cfg, d_tab, hg, len(counts), arena, H, 41,
+                   pbm.LAUNCH_PLAIN if mode == "plain" else pbm.LAUNCH_PERSISTENT, results=res)
+    torch.cuda.synchronize()
+    st = pool.stats()
+    assert st.failures == 0 and st.successes == N == st.frees
+    a = arena.cpu().numpy()
+    assert np.array_equal(res.cpu().numpy(), a[:N])          # request q's page sits in slot q
+    assert (a[:N] != held[:N]).all() and np.array_equal(a[N:], held[N:])
+    chk = pool.check(arena, H)
+    assert chk.n_duplicates == 0 and chk.n_not_marked == 0 and chk.used_pages == H
+    pool.close()

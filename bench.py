@@ -498,10 +498,11 @@ def _ev_ms(torch, stream, fn):
     return e0.elapsed_time(e1)
 
 
-def config_claim_write_free(torch, pbm, stream, reps=200):
+def config_claim_write_free(torch, pbm, stream, reps=200, cpu=True):
     """65,536 pages x 64 B (2,048-word bitmap) at 50% occupancy (seed 1);
     32,768 threads (seed 1 + tid) each claim a page with the page-probe walk,
-    write their tid into its 64-B payload and free it."""
+    write their tid into its 64-B payload and free it.  `cpu`: also time the
+    std::atomic host replay of the same requests on the same bitmap."""
     sh = stream.cuda_stream
     T, N = 1 << 16, 1 << 15
     out = {}
@@ -523,6 +524,17 @@ def config_claim_write_free(torch, pbm, stream, reps=200):
            "bitmap_restored": bool(np.array_equal(before, after)),
            "note": "L2-resident (8 KiB bitmap, 4 MiB pages); median launch time over the launches"}
     pool.close()
+    if cpu:
+        import oracle
+
+        secs, ok, _, th = oracle.cpu_claim_write_free(before.copy(), T, 64, 64, N, 1, 20)
+        passes = int(min(100000, max(20, 20 * 3.0 / max(secs, 1e-3))))
+        w = before.copy()
+        secs, ok, st, th = oracle.cpu_claim_write_free(w, T, 64, 64, N, 1, passes)
+        out["cpu_replay"] = {"value": 2 * ok / secs, "unit": "ops/s", "cores": th, "kind": "port",
+                             "mean_steps": st / max(1, ok), "bitmap_restored": bool(np.array_equal(w, before)),
+                             "sample": f"{passes} passes over the {N} requests on the same bitmap, page-probe walk, "
+                                       f"std::atomic on {th} host threads, {secs:.1f} s"}
     return out
 
 
@@ -795,7 +807,8 @@ def config_serving(torch, pbm, stream, rates=(1e5, 1e6, 1e7, 1e8, 1e9), min_req=
 
 def run_configs(args, torch, pbm, stream):
     flush = torch.empty(512 << 20, dtype=torch.uint8, device="cuda")
-    todo = [("claim_write_free_50pct", lambda: config_claim_write_free(torch, pbm, stream)),
+    todo = [("claim_write_free_50pct", lambda: config_claim_write_free(torch, pbm, stream,
+                                                                      cpu=not args.no_cpu_baseline)),
             ("occupancy_sweep", lambda: config_occupancy_sweep(torch, pbm, stream, flush)),
             ("buffer_manager", lambda: config_buffer_manager(torch, pbm, stream, flush)),
             ("malloc", lambda: config_malloc(torch, pbm, stream, flush)),

@@ -116,6 +116,55 @@ double orc_cpu_churn(uint32_t* words, uint64_t n_pages, int32_t* held, uint64_t 
     return std::chrono::duration<double>(t1 - t0).count();
 }
 
+// Claim, write, free (the 64-byte-page workload, unitTest1.5.cu:127-150 with
+// getPagePtr payloads): request i claims a page with the page-probe walk,
+// writes i into the first payload_bytes of the page and frees it at once;
+// `reps` passes over the n requests, split evenly over `threads` host threads.
+// Returns wall seconds of the parallel region; ok/steps are totals.
+double orc_cpu_claim_write_free(uint32_t* words, uint64_t n_pages, uint8_t* pages, uint32_t page_size,
+                                uint32_t payload_bytes, uint64_t n, uint32_t seed, int threads, uint32_t reps,
+                                uint32_t max_steps, uint64_t* ok, uint64_t* steps) {
+    if (threads < 1) threads = 1;
+    const uint32_t T = (uint32_t)n_pages;
+    const uint32_t words_per = payload_bytes / 4u;
+    std::vector<uint64_t> oks(threads), stps(threads);
+    std::atomic<int> ready{0};
+    std::atomic<bool> go{false};
+    auto body = [&](int t) {
+        const uint64_t lo = n * (uint64_t)t / (uint64_t)threads;
+        const uint64_t hi = n * (uint64_t)(t + 1) / (uint64_t)threads;
+        uint64_t o = 0, st = 0;
+        ready.fetch_add(1);
+        while (!go.load(std::memory_order_acquire)) {}
+        for (uint32_t r = 0; r < reps; ++r) {
+            for (uint64_t i = lo; i < hi; ++i) {
+                uint32_t s = 0;
+                const int32_t id = walk_page(words, T, orc_seed(seed, (uint32_t)i), max_steps, &s);
+                st += s;
+                if (id < 0) continue;
+                ++o;
+                int32_t* pg = reinterpret_cast<int32_t*>(pages + (uint64_t)(uint32_t)id * page_size);
+                for (uint32_t k = 0; k < words_per; ++k) __atomic_store_n(pg + k, (int32_t)i, __ATOMIC_RELAXED);
+                __atomic_fetch_and(words + ((uint32_t)id >> 5), ~(1u << ((uint32_t)id & 31u)), __ATOMIC_RELEASE);
+            }
+        }
+        oks[t] = o;
+        stps[t] = st;
+    };
+    std::vector<std::thread> pool;
+    for (int t = 0; t < threads; ++t) pool.emplace_back(body, t);
+    while (ready.load() < threads) {}
+    auto t0 = std::chrono::steady_clock::now();
+    go.store(true, std::memory_order_release);
+    for (auto& th : pool) th.join();
+    auto t1 = std::chrono::steady_clock::now();
+    uint64_t O = 0, S = 0;
+    for (int t = 0; t < threads; ++t) { O += oks[t]; S += stps[t]; }
+    if (ok) *ok = O;
+    if (steps) *steps = S;
+    return std::chrono::duration<double>(t1 - t0).count();
+}
+
 int orc_hw_threads(void) {
     unsigned n = std::thread::hardware_concurrency();
     return n ? (int)n : 1;

@@ -60,6 +60,8 @@ SIGS = [
     ("orc_ref_dist_clock_arm", c_int32, [c_int32, c_int16, c_int32]),
     ("orc_cpu_churn", c_double, [_P, c_uint64, _P, c_uint64, c_uint64, c_uint32, c_int, c_int, c_uint32,
                                  POINTER(c_uint64), POINTER(c_uint64), POINTER(c_uint64)]),
+    ("orc_cpu_claim_write_free", c_double, [_P, c_uint64, _P, c_uint32, c_uint32, c_uint64, c_uint32, c_int,
+                                            c_uint32, c_uint32, POINTER(c_uint64), POINTER(c_uint64)]),
     ("orc_hw_threads", c_int, []),
 ]
 
@@ -224,6 +226,20 @@ def cpu_churn(words, n_pages, held, n_pairs, seed, threads=None, walk=1, max_ste
     secs = L.orc_cpu_churn(P(words), n_pages, P(held), len(held), n_pairs, seed, threads, walk, max_steps,
                            ctypes.byref(ok), ctypes.byref(fail), ctypes.byref(st))
     return secs, ok.value, fail.value, st.value, threads
+
+
+def cpu_claim_write_free(words, n_pages, page_size, payload_bytes, n, seed, reps, threads=None, max_steps=4096):
+    """std::atomic host replay of claim/write/free; returns (seconds, ok, steps, threads)."""
+    import numpy as np
+
+    L = lib()
+    if threads is None:
+        threads = L.orc_hw_threads()
+    pages = np.zeros(int(n_pages) * int(page_size), dtype=np.uint8)
+    ok, st = c_uint64(), c_uint64()
+    secs = L.orc_cpu_claim_write_free(P(words), n_pages, P(pages), page_size, payload_bytes, n, seed, threads,
+                                      reps, max_steps, ctypes.byref(ok), ctypes.byref(st))
+    return secs, ok.value, st.value, threads
 
 
 def fifo_replay(free_pages_sorted, ops):

@@ -269,6 +269,9 @@ void orc_qmalloc_free_group(orc_qmalloc_t *q, const int64_t *offsets, int lanes,
 double orc_cpu_churn(uint32_t *words, uint64_t n_pages, int32_t *held, uint64_t n_held,
                      uint64_t n_pairs, uint32_t seed, int threads, int walk, uint32_t max_steps,
                      uint64_t *ok, uint64_t *fail, uint64_t *steps);
+double orc_cpu_claim_write_free(uint32_t *words, uint64_t n_pages, uint8_t *pages, uint32_t page_size,
+                                uint32_t payload_bytes, uint64_t n, uint32_t seed, int threads, uint32_t reps,
+                                uint32_t max_steps, uint64_t *ok, uint64_t *steps);
 int orc_hw_threads(void);
 
 #ifdef __cplusplus

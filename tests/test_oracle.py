@@ -164,6 +164,15 @@ def test_cpu_churn_keeps_occupancy(orc):
     assert np.unique(held).size == held.size
 
 
+def test_cpu_claim_write_free_restores_bitmap(orc):
+    T, N = 1 << 16, 1 << 12
+    words = orc.bernoulli_bitmap(T, 0.5, 1)
+    before = words.copy()
+    secs, ok, steps, threads = orc.cpu_claim_write_free(words, T, 64, 64, N, 1, 3, threads=2)
+    assert ok == 3 * N and steps >= ok and secs > 0 and threads == 2
+    assert np.array_equal(words, before)
+
+
 def test_malloc_replay_blocks_and_release(orc):
     """The malloc replay packs sub-page blocks aligned to their class, gives
     larger blocks their own runs, and the last free of a run releases it."""

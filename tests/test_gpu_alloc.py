@@ -179,6 +179,60 @@ def test_word_probe_steps_match_rwbm_tas(cuda, pbm_mod, orc, occ):
     pool.close()
 
 
+@pytest.mark.parametrize("strategy,T,occ", [(0, 1 << 20, 0.9), (1, 1 << 22, 0.9), (1, 1 << 22, 0.95),
+                                            (1, 1 << 22, 0.97)])
+def test_per_warp_max_steps_within_was_models(cuda, pbm_mod, orc, strategy, T, occ):
+    """RW_WAS / RWBM_WAS: the mean over warps of the per-warp maximum of the
+    steps (unitTests/metrics.h:23-31) lies between the model at the batch's
+    starting occupancy (A free) and at its final one (A - N free), within 3 SE.
+    N is small against the words (the word-probe model assumes independent
+    bits, which claims piling into the same words break)."""
+    import models
+
+    torch = cuda
+    pbm = pbm_mod
+    N = 4096
+    pool = _pool(pbm, T, occ, 2)
+    A = T - pool.used()
+    ids = torch.empty(N, dtype=torch.int32, device="cuda")
+    st = torch.empty(N, dtype=torch.int32, device="cuda")
+    pool.alloc(pbm.walk_config(strategy), N, 5, ids, st)
+    assert (ids.cpu().numpy() >= 0).all()
+    m, se = _mean_se(st.cpu().numpy().reshape(-1, 32).max(axis=1))
+    model = models.rw_was if strategy == 0 else models.rwbm_was
+    lo, hi = model(T, A, 0), model(T, A, N)
+    assert lo - 3 * se <= m <= hi + 3 * se, (m, se, lo, hi)
+    pool.close()
+
+
+@pytest.mark.parametrize("occ", [0.8, 0.9])
+def test_collab_warp_steps_match_corwbm_was(cuda, pbm_mod, orc, occ):
+    """CoRWBM_WAS (warp steps of the collaborative walk, 32 lanes): where the
+    window's expected free bits cover the warp (80-90% occupancy) the model
+    gives one jump; measured within 3 SE (plus 0.01 for the rare warp that
+    loses bits to a concurrent grab).  At 95% and above the model's normal
+    approximation undershoots the walk (1.2 vs 1.66 jumps at 97% in the
+    oracle's replay), so it is not checked there."""
+    pytest.importorskip("mpmath")
+    import models
+
+    torch = cuda
+    pbm = pbm_mod
+    T, N = 1 << 20, 4096
+    pool = _pool(pbm, T, occ, 2)
+    A = T - pool.used()
+    ids = torch.empty(N, dtype=torch.int32, device="cuda")
+    st = torch.empty(N, dtype=torch.int32, device="cuda")
+    pool.alloc(pbm.walk_config(pbm.COLLAB_RW_BM, collab_width=32), N, 5, ids, st)
+    assert (ids.cpu().numpy() >= 0).all()
+    warp = st.cpu().numpy().reshape(-1, 32)
+    assert (warp == warp[:, :1]).all()            # every lane reports its warp's jumps
+    m, se = _mean_se(warp[:, 0])
+    pred = models.corwbm_was(T, A, N)
+    assert abs(m - pred) <= 3 * se + 0.01, (m, se, pred)
+    pool.close()
+
+
 def test_config1_claim_write_free(cuda, pbm_mod, orc):
     """Config 1 as written: 32,768 requests on a 65,536-page pool at 50%
     (seed 1) each claim one page, write their index into its 64-B payload,

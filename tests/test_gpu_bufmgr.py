@@ -93,7 +93,8 @@ def test_parallel_rounds_invariants_and_copy(cuda, pbm_mod, policy, n_arms):
 def test_parallel_rounds_fewer_frames_than_a_warp(cuda, pbm_mod, policy, n_arms):
     """16 frames, so one warp's sweep batch wraps the frames twice (two lanes
     examine each frame) and most fetches find every frame pinned: fetches
-    fail after their bounded sweep, and the maps stay consistent."""
+    fail after their bounded sweep (or give up a bounded wait on a page
+    another request is loading), and the maps stay consistent."""
     torch = cuda
     pbm = pbm_mod
     n_logical, n_frames, rounds, R = 256, 16, 12, 256
@@ -114,7 +115,7 @@ def test_parallel_rounds_fewer_frames_than_a_warp(cuda, pbm_mod, policy, n_arms)
         held = (~released[:(r + 1) * R]) & (fr >= 0)
         assert chk.pins == int(held.sum())
     c = bm.counters()
-    assert c.bad_unpins == 0 and c.timeouts == 0
-    assert c.hits + c.misses + c.failures == rounds * R
+    assert c.bad_unpins == 0
+    assert c.hits + c.misses + c.failures + c.timeouts == rounds * R
     assert c.failures > 0 and c.misses > 0
     bm.close()

@@ -1,5 +1,5 @@
 // cpu_replay.cpp -- std::atomic host replay of the reference's bitmap random
-// walks (the CPU baseline; TEST INFRASTRUCTURE / BASELINE ONLY).
+// walks (the CPU baseline; TEST INFRASTRUCTURE / CPU BASELINE ONLY).
 //
 // Restates, on host threads, the per-thread walks of
 //   source/RandomWalkBasic_BM.cuh:60-102  (word probe: random word, claim its

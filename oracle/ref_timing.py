@@ -1,6 +1,6 @@
 """Times the reference's own CUDA build on the alloc+free churn workload.
 
-TEST INFRASTRUCTURE / BASELINE ONLY.  Runs the reference's getPage and
+TEST INFRASTRUCTURE / REFERENCE TIMING ONLY.  Runs the reference's getPage and
 freePage (CollabRW_BM.cuh:114-160 and :73-77, the warp-collaborative walk; or
 RandomWalkBasic.cuh:52-83, the page-probe walk on an int-per-page map) from
 the cubins that `make ref` builds from its unchanged sources, through the

@@ -259,7 +259,13 @@ int pbm_server_run(pbm_server* s, const pbm_request* reqs, uint64_t n, pbm_reque
             rr = (rr + 1u) % s->cfg.n_tenants;
             if (nreq) {
                 cudaStream_t st = slot->stream;
-                if (ng) {
+                if (ng <= PBM_MAX_INLINE_GROUPS) {
+                    // the batch's table rides in the launch: no copy ahead of it
+                    if (ng) rc = pbm_batch_launch(s->pool, &s->cfg.walk, nullptr, slot->h_groups, ng, s->d_rings,
+                                                  (uint64_t)s->cfg.n_tenants * R, s->seed++, nullptr,
+                                                  PBM_LAUNCH_PERSISTENT, st);
+                    if (rc) return rc;
+                } else {
                     PBM_CUDA_TRY(cudaMemcpyAsync(slot->d_groups, slot->h_groups, ng * sizeof(pbm_group),
                                                  cudaMemcpyHostToDevice, st));
                     rc = pbm_batch_launch(s->pool, &s->cfg.walk, slot->d_groups, nullptr, ng, s->d_rings,

@@ -312,28 +312,34 @@ int persistent_blocks_per_sm(int block) {
 // >= kCappedBlocks: the variant whose registers are capped for kCappedBlocks
 // resident blocks (5 x 256 threads: at most 51 registers, no spills for the
 // collaborative walk on 32-bit words).
+// grid_cap > 0: at most that many blocks (a batch whose size the host knows
+// and that needs fewer blocks than fill the GPU).
 template <BWalk K, int W, typename Word, typename Tab>
 void launch_persistent(const BatchArgs& a, const Tab& tab, int block, int blocks_per_sm, size_t smem,
-                       cudaStream_t s) {
+                       cudaStream_t s, unsigned grid_cap) {
+    auto grid_of = [&](int per_sm) {
+        const unsigned g = (unsigned)(sm_count() * per_sm);
+        return grid_cap && grid_cap < g ? grid_cap : g;
+    };
     if (blocks_per_sm >= kCappedBlocks) {
         int fit = persistent_blocks_per_sm<K, W, Word, kCappedBlocks, Tab>(block);
         int per_sm = blocks_per_sm < fit ? blocks_per_sm : fit;
-        k_batch_persistent<K, W, Word, kCappedBlocks, Tab><<<sm_count() * per_sm, block, smem, s>>>(a, tab);
+        k_batch_persistent<K, W, Word, kCappedBlocks, Tab><<<grid_of(per_sm), block, smem, s>>>(a, tab);
     } else {
         int fit = persistent_blocks_per_sm<K, W, Word, 1, Tab>(block);
         int per_sm = (blocks_per_sm > 0 && blocks_per_sm < fit) ? blocks_per_sm : fit;
-        k_batch_persistent<K, W, Word, 1, Tab><<<sm_count() * per_sm, block, smem, s>>>(a, tab);
+        k_batch_persistent<K, W, Word, 1, Tab><<<grid_of(per_sm), block, smem, s>>>(a, tab);
     }
 }
 
 // tab: the inline descriptor table of a launch-form batch (null: a.groups).
 template <BWalk K, int W, typename Word>
 int launch_batch_kw(const BatchArgs& a, bool persistent, int block, int blocks_per_sm, cudaStream_t s,
-                    const GroupTable* tab) {
+                    const GroupTable* tab, unsigned grid_cap) {
     if (persistent) {
         const size_t smem = a.fuse ? sizeof(unsigned long long) * (a.n_groups + 1u) : 0u;
-        if (tab) launch_persistent<K, W, Word>(a, *tab, block, blocks_per_sm, smem, s);
-        else launch_persistent<K, W, Word>(a, NoTable{}, block, blocks_per_sm, smem, s);
+        if (tab) launch_persistent<K, W, Word>(a, *tab, block, blocks_per_sm, smem, s, grid_cap);
+        else launch_persistent<K, W, Word>(a, NoTable{}, block, blocks_per_sm, smem, s, grid_cap);
     } else {
         const unsigned long long per_warp = 32ull * kReqPerLane<K>;
         unsigned long long warps = (a.count + per_warp - 1ull) / per_warp;
@@ -346,26 +352,26 @@ int launch_batch_kw(const BatchArgs& a, bool persistent, int block, int blocks_p
 }
 
 int launch_batch(const pbm_walk_config* c, const BatchArgs& a, bool persistent, cudaStream_t s,
-                 const GroupTable* tab = nullptr) {
+                 const GroupTable* tab = nullptr, unsigned grid_cap = 0) {
     const int block = c->block_size ? c->block_size : kDefaultBlock;
     const int bps = c->blocks_per_sm;
     const bool w64 = c->word_bits == 64;
     switch (c->strategy) {
     case PBM_RANDOM_WALK:
-        return launch_batch_kw<BWalk::Page, 32, uint32_t>(a, persistent, block, bps, s, tab);
+        return launch_batch_kw<BWalk::Page, 32, uint32_t>(a, persistent, block, bps, s, tab, grid_cap);
     case PBM_RANDOM_WALK_BM:
-        return w64 ? launch_batch_kw<BWalk::Word64, 32, uint64_t>(a, persistent, block, bps, s, tab)
-                   : launch_batch_kw<BWalk::Word32, 32, uint32_t>(a, persistent, block, bps, s, tab);
+        return w64 ? launch_batch_kw<BWalk::Word64, 32, uint64_t>(a, persistent, block, bps, s, tab, grid_cap)
+                   : launch_batch_kw<BWalk::Word32, 32, uint32_t>(a, persistent, block, bps, s, tab, grid_cap);
     case PBM_COLLAB_RW_BM: {
         const int W = c->collab_width ? c->collab_width : 32;
-        if (W == 64) return w64 ? launch_batch_kw<BWalk::Collab2, 32, uint64_t>(a, persistent, block, bps, s, tab)
-                                : launch_batch_kw<BWalk::Collab2, 32, uint32_t>(a, persistent, block, bps, s, tab);
-        if (W == 8) return w64 ? launch_batch_kw<BWalk::Collab, 8, uint64_t>(a, persistent, block, bps, s, tab)
-                               : launch_batch_kw<BWalk::Collab, 8, uint32_t>(a, persistent, block, bps, s, tab);
-        if (W == 16) return w64 ? launch_batch_kw<BWalk::Collab, 16, uint64_t>(a, persistent, block, bps, s, tab)
-                                : launch_batch_kw<BWalk::Collab, 16, uint32_t>(a, persistent, block, bps, s, tab);
-        return w64 ? launch_batch_kw<BWalk::Collab, 32, uint64_t>(a, persistent, block, bps, s, tab)
-                   : launch_batch_kw<BWalk::Collab, 32, uint32_t>(a, persistent, block, bps, s, tab);
+        if (W == 64) return w64 ? launch_batch_kw<BWalk::Collab2, 32, uint64_t>(a, persistent, block, bps, s, tab, grid_cap)
+                                : launch_batch_kw<BWalk::Collab2, 32, uint32_t>(a, persistent, block, bps, s, tab, grid_cap);
+        if (W == 8) return w64 ? launch_batch_kw<BWalk::Collab, 8, uint64_t>(a, persistent, block, bps, s, tab, grid_cap)
+                               : launch_batch_kw<BWalk::Collab, 8, uint32_t>(a, persistent, block, bps, s, tab, grid_cap);
+        if (W == 16) return w64 ? launch_batch_kw<BWalk::Collab, 16, uint64_t>(a, persistent, block, bps, s, tab, grid_cap)
+                                : launch_batch_kw<BWalk::Collab, 16, uint32_t>(a, persistent, block, bps, s, tab, grid_cap);
+        return w64 ? launch_batch_kw<BWalk::Collab, 32, uint64_t>(a, persistent, block, bps, s, tab, grid_cap)
+                   : launch_batch_kw<BWalk::Collab, 32, uint32_t>(a, persistent, block, bps, s, tab, grid_cap);
     }
     default:
         return PBM_ERR_UNSUPPORTED;
@@ -467,13 +473,21 @@ int pbm_batch_launch_results(pbm_pool* pool, const pbm_walk_config* cfg, const p
     if (!d_groups) {                   // host table carried in the launch's parameters
         if (!h_groups || n_groups > PBM_MAX_INLINE_GROUPS) return PBM_ERR_INVALID;
         GroupTable tab{};
+        unsigned long long total = 0;
         for (uint32_t g = 0; g < n_groups; ++g) {
             if (h_groups[g].op < PBM_OP_ALLOC || h_groups[g].op > PBM_OP_SWAP) return PBM_ERR_INVALID;
             tab.g[g] = h_groups[g];
+            total += h_groups[g].count;
         }
+        if (total == 0) return PBM_OK;
         a.n_groups = n_groups;
         a.fuse = 1;
-        return launch_batch(cfg, a, true, s, &tab);
+        // the host knows the batch's size: no more blocks than chunks for one
+        // chunk per warp (a small batch launches one block, not a full grid)
+        const unsigned long long per_chunk = (cfg->strategy == PBM_COLLAB_RW_BM && cfg->collab_width == 64) ? 64ull : 32ull;
+        const unsigned long long warps = (unsigned long long)(cfg->block_size ? cfg->block_size : kDefaultBlock) / 32ull;
+        const unsigned long long need = ((total + per_chunk - 1ull) / per_chunk + warps - 1ull) / warps;
+        return launch_batch(cfg, a, true, s, &tab, (unsigned)(need < 0xffffffffull ? need : 0xffffffffull));
     }
     a.groups = d_groups;
     a.n_groups = n_groups;

@@ -765,11 +765,14 @@ def config_malloc(torch, pbm, stream, flush, rounds=16, plain_rounds=4, max_step
     return out
 
 
-def config_serving(torch, pbm, stream, rates=(1e5, 1e6, 1e7, 1e8, 1e9), min_req=100, max_req=20000,
+def config_serving(torch, pbm, stream, rates=(1e5, 1e6, 1e7, 1e8, 1e9, 1e10, 1e11), min_req=100, max_req=20000,
                    horizon_s=1.0):
     """64 tenants, Poisson arrivals at an aggregate page rate, batches
     LogU[1,65536] pages, mix 45% alloc / 45% free / 10% Zipf(0.99) fetch,
-    seed 5; 2^24-page pool prefilled to 80%, budget 95%."""
+    seed 5; 2^24-page pool prefilled to 80%, budget 95%.  The rates past
+    1e9 (the workload's range) look for the loop's capacity: where the wall
+    time exceeds the arrival span, throughput is the saturation rate and the
+    latencies include queueing."""
     import workloads
 
     T = T_PAGES

@@ -657,6 +657,20 @@ __host__ __device__ __forceinline__ uint32_t span_mask(uint32_t p0, uint32_t n, 
     return bit_range(ww == a ? (p0 & 31u) : 0u, ww == b ? ((p0 + n - 1u) & 31u) : 31u);
 }
 
+// First run of n <= 32 free pages in words w (value v0) and w+1 (value v1,
+// all ones past the last word): inside w, across the boundary, inside w+1.
+__device__ __forceinline__ int32_t span_in_pair(uint32_t w, uint32_t v0, uint32_t v1, uint32_t n, uint32_t L) {
+    uint32_t r = run_starts(~v0, n);
+    if (r) return (int32_t)(w * 32u + (uint32_t)(__ffs((int)r) - 1));
+    const uint32_t hi = v0 ? (uint32_t)__clz((int)v0) : 32u;
+    if (w + 1u >= L) return -1;
+    const uint32_t lo = v1 ? (uint32_t)(__ffs((int)v1) - 1) : 32u;
+    if (hi > 0u && hi + lo >= n) return (int32_t)(w * 32u + 32u - hi);
+    r = run_starts(~v1, n);
+    if (r) return (int32_t)((w + 1u) * 32u + (uint32_t)(__ffs((int)r) - 1));
+    return -1;
+}
+
 // First run of n free pages seen from word w on (-1 if none in the window).
 __device__ __forceinline__ int32_t find_span(const PoolView& v, uint32_t w, uint32_t n) {
     const uint32_t L = v.n_words32;
@@ -664,15 +678,7 @@ __device__ __forceinline__ int32_t find_span(const PoolView& v, uint32_t w, uint
         // two-word window, both loads in flight together (same result as the loop below)
         const uint32_t v0 = load_word(v.words + w);
         const uint32_t v1 = w + 1u < L ? load_word(v.words + w + 1u) : kFull32;
-        uint32_t r = run_starts(~v0, n);
-        if (r) return (int32_t)(w * 32u + (uint32_t)(__ffs((int)r) - 1));
-        const uint32_t hi = v0 ? (uint32_t)__clz((int)v0) : 32u;
-        if (w + 1u >= L) return -1;
-        const uint32_t lo = v1 ? (uint32_t)(__ffs((int)v1) - 1) : 32u;
-        if (hi > 0u && hi + lo >= n) return (int32_t)(w * 32u + 32u - hi);
-        r = run_starts(~v1, n);
-        if (r) return (int32_t)((w + 1u) * 32u + (uint32_t)(__ffs((int)r) - 1));
-        return -1;
+        return span_in_pair(w, v0, v1, n, L);
     }
     const uint32_t nscan = (n + 31u) / 32u + 1u;
     uint32_t run = 0, start = 0;   // free pages ending at the top of the previous word
@@ -702,31 +708,79 @@ __device__ __forceinline__ void free_span(const PoolView& v, int32_t id, uint32_
     for (uint32_t ww = p0 >> 5; ww <= (p0 + n - 1u) >> 5; ++ww) atomicAnd(v.words + ww, ~span_mask(p0, n, ww));
 }
 
+// Claims the run of n pages at p0 word by word; on a word that lost bits to
+// another claim, every bit this claim set is released again.
+__device__ __forceinline__ bool claim_span(const PoolView& v, uint32_t p0, uint32_t n) {
+    const uint32_t a = p0 >> 5, b = (p0 + n - 1u) >> 5;
+    uint32_t ww = a;
+    for (; ww <= b; ++ww) {
+        const uint32_t m = span_mask(p0, n, ww);
+        const uint32_t old = atomicOr(v.words + ww, m);
+        if (old & m) {                                   // lost part of the run
+            if (m & ~old) atomicAnd(v.words + ww, ~(m & ~old));
+            break;
+        }
+    }
+    if (ww > b) return true;
+    for (uint32_t k = a; k < ww; ++k) atomicAnd(v.words + k, ~span_mask(p0, n, k));   // roll back
+    return false;
+}
+
+// Random jumps until a run of n free pages is claimed (steps = jumps).  For
+// n <= 32 the walk is pipelined: the LCG fixes every jump's words in
+// advance, so the next kSpanAhead jumps' two words are in flight while a
+// jump is judged and claimed, and the same words are examined in the same
+// order.  Measured on the malloc workload (GB300): 1.64 G ops/s one jump
+// ahead, 1.46 two ahead, 1.41 three ahead, 1.36 unpipelined.
+constexpr int kSpanAhead = 1;
 __device__ __forceinline__ int32_t walk_span(const PoolView& v, uint32_t n, int32_t seed0,
                                              uint32_t max_steps, int32_t* steps_out) {
     const uint32_t L = v.n_words32;
     int32_t x = seed0 & 0x7fffffff;   // walks run on 31-bit states
     uint32_t s = 0;
+    if (n <= 32u && max_steps > 0u) {
+        // ring of the next kSpanAhead jumps' words, loads in flight
+        uint32_t pw[kSpanAhead], p0[kSpanAhead], p1[kSpanAhead];
+#pragma unroll
+        for (int k = 0; k < kSpanAhead; ++k) {
+            x = lcg31(x);
+            pw[k] = idx_hi(x, L);
+            p0[k] = (uint32_t)k < max_steps ? load_word(v.words + pw[k]) : kFull32;
+            p1[k] = (uint32_t)k < max_steps && pw[k] + 1u < L ? load_word(v.words + pw[k] + 1u) : kFull32;
+        }
+        while (s < max_steps) {
+            const uint32_t w = pw[0], v0 = p0[0], v1 = p1[0];
+            ++s;
+#pragma unroll
+            for (int k = 0; k + 1 < kSpanAhead; ++k) {
+                pw[k] = pw[k + 1];
+                p0[k] = p0[k + 1];
+                p1[k] = p1[k + 1];
+            }
+            x = lcg31(x);                                  // jump s + kSpanAhead
+            pw[kSpanAhead - 1] = idx_hi(x, L);
+            const bool more = s + (uint32_t)kSpanAhead <= max_steps;
+            p0[kSpanAhead - 1] = more ? load_word(v.words + pw[kSpanAhead - 1]) : kFull32;
+            p1[kSpanAhead - 1] = more && pw[kSpanAhead - 1] + 1u < L ? load_word(v.words + pw[kSpanAhead - 1] + 1u)
+                                                                     : kFull32;
+            const int32_t found = span_in_pair(w, v0, v1, n, L);
+            if (found >= 0 && claim_span(v, (uint32_t)found, n)) {
+                if (steps_out) *steps_out = (int32_t)s;
+                return found;
+            }
+        }
+        if (steps_out) *steps_out = (int32_t)s;
+        return -1;
+    }
     while (s < max_steps) {
         ++s;
         x = lcg31(x);
         const int32_t found = find_span(v, idx_hi(x, L), n);
         if (found < 0) continue;
-        const uint32_t p0 = (uint32_t)found, a = p0 >> 5, b = (p0 + n - 1u) >> 5;
-        uint32_t ww = a;
-        for (; ww <= b; ++ww) {
-            const uint32_t m = span_mask(p0, n, ww);
-            const uint32_t old = atomicOr(v.words + ww, m);
-            if (old & m) {                                   // lost part of the run
-                if (m & ~old) atomicAnd(v.words + ww, ~(m & ~old));
-                break;
-            }
-        }
-        if (ww > b) {
+        if (claim_span(v, (uint32_t)found, n)) {
             if (steps_out) *steps_out = (int32_t)s;
             return found;
         }
-        for (uint32_t k = a; k < ww; ++k) atomicAnd(v.words + k, ~span_mask(p0, n, k));   // roll back
     }
     if (steps_out) *steps_out = (int32_t)s;
     return -1;

@@ -786,6 +786,81 @@ __device__ __forceinline__ int32_t walk_span(const PoolView& v, uint32_t n, int3
     return -1;
 }
 
+// Runs of need_n <= 32 pages (0 = none) for the lanes of a whole warp, each
+// lane on its own LCG sequence from seed0; steps = jumps.  Every needing
+// lane first takes one jump of its own (all in parallel).  Each lane still
+// unserved is then walked by the whole warp, 32 of its jumps at a time:
+// lane j judges the lane's jump s + j + 1 (its LCG state advanced j + 1
+// steps at once) and the runs found are claimed in jump order.  In a run
+// without races a lane gets the page the one-lane walk would give it, after
+// the same jumps; a walk that keeps missing costs max_steps / 32 rounds
+// instead of max_steps jumps.  The whole warp calls converged.
+__device__ __forceinline__ int32_t walk_span_warp(const PoolView& v, uint32_t need_n, int32_t seed0,
+                                                  uint32_t max_steps, int32_t* steps_out) {
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t L = v.n_words32;
+    int32_t x = seed0 & 0x7fffffff;   // walks run on 31-bit states
+    uint32_t s = 0;
+    int32_t id = -1;
+    if (need_n > 0u && max_steps > 0u) {
+        s = 1;
+        x = lcg31(x);
+        const uint32_t w = idx_hi(x, L);
+        const uint32_t v0 = load_word(v.words + w);
+        const uint32_t v1 = w + 1u < L ? load_word(v.words + w + 1u) : kFull32;
+        const int32_t f = span_in_pair(w, v0, v1, need_n, L);
+        if (f >= 0 && claim_span(v, (uint32_t)f, need_n)) id = f;
+    }
+    // this lane's jump ahead by lane + 1 LCG steps: x -> (aj * x + cj) mod 2^31
+    uint32_t aj = 1103515245u, cj = 12345u;
+    for (uint32_t k = 0; k < lane; ++k) {
+        cj = 1103515245u * cj + 12345u;
+        aj *= 1103515245u;
+    }
+    uint32_t pend = __ballot_sync(kFull32, need_n > 0u && id < 0 && s < max_steps);
+    while (pend) {
+        const int l0 = __ffs((int)pend) - 1;
+        const uint32_t x0 = (uint32_t)__shfl_sync(kFull32, x, l0);
+        const uint32_t n0 = __shfl_sync(kFull32, need_n, l0);
+        const uint32_t s0 = __shfl_sync(kFull32, s, l0);
+        const int32_t xj = (int32_t)((aj * x0 + cj) & 0x7fffffffu);
+        const uint32_t wj = idx_hi(xj, L);
+        int32_t fj = -1;
+        if (s0 + lane + 1u <= max_steps) {
+            const uint32_t a0 = load_word(v.words + wj);
+            const uint32_t a1 = wj + 1u < L ? load_word(v.words + wj + 1u) : kFull32;
+            fj = span_in_pair(wj, a0, a1, n0, L);
+        }
+        uint32_t cm = __ballot_sync(kFull32, fj >= 0);
+        int32_t got = -1;
+        uint32_t used = 32u;
+        while (cm) {                                       // claims in jump order
+            const int j = __ffs((int)cm) - 1;
+            cm &= cm - 1u;
+            bool ok = false;
+            if ((int)lane == j) ok = claim_span(v, (uint32_t)fj, n0);
+            if (__shfl_sync(kFull32, ok, j)) {
+                got = __shfl_sync(kFull32, fj, j);
+                used = (uint32_t)j + 1u;
+                break;
+            }
+        }
+        const int32_t x_last = __shfl_sync(kFull32, xj, 31);   // the state 32 jumps on
+        if ((int)lane == l0) {
+            if (got >= 0) {
+                id = got;
+                s = s0 + used;
+            } else {
+                s = s0 + 32u < max_steps ? s0 + 32u : max_steps;
+                x = x_last;
+            }
+        }
+        pend = __ballot_sync(kFull32, need_n > 0u && id < 0 && s < max_steps);
+    }
+    if (steps_out) *steps_out = (int32_t)s;
+    return id;
+}
+
 // ---------------------------------------------------------------------------
 // FIFO free list (linked-list strategy, parallelPage.cu:342-440, restated
 // lock-free).  get: reserve one free page on `avail`, take a head ticket,

@@ -78,6 +78,32 @@ __device__ __forceinline__ void* malloc_group(const MallocView& m, uint32_t acti
     }
     void* out = nullptr;
     const uint32_t small_mask = __ballot_sync(active, small);
+    if (!serial_large && active == kFull32) {
+        // the whole warp walks for the group's small run (its first small lane
+        // asks for it) and the large runs together: one jump each, then 32
+        // jumps at a time for each run still unserved; runs of more than 32
+        // pages walk on their own
+        const int leader = small_mask ? __ffs((int)small_mask) - 1 : -1;
+        uint32_t need = 0u;
+        int32_t seed = seed_own;
+        if (large) {
+            need = bytes >> m.page_shift;
+        } else if ((int)lane == leader) {
+            need = (total + page - 1u) >> m.page_shift;
+            seed = seed_small;
+        }
+        int32_t s = 0;
+        int32_t start = walk_span_warp(m.pool, need <= 32u ? need : 0u, seed, max_steps, &s);
+        if (need > 32u) start = walk_span(m.pool, need, seed, max_steps, &s);
+        if (need) steps = s;
+        if (start >= 0) malloc_mark_run(m, start, need, large ? 1 : __popc(small_mask));
+        const int32_t small_start = __shfl_sync(kFull32, start, leader >= 0 ? leader : 0);
+        if (small && small_start >= 0)
+            out = (void*)(m.pool.base + ((size_t)(uint32_t)small_start << m.page_shift) + offset);
+        if (large && start >= 0) out = (void*)(m.pool.base + ((size_t)(uint32_t)start << m.page_shift));
+        if (steps_out) *steps_out = steps;
+        return out;
+    }
     if (small_mask) {
         const int leader = __ffs((int)small_mask) - 1;
         int32_t start = -1;

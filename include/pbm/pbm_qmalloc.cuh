@@ -112,14 +112,12 @@ __device__ __forceinline__ void* q_handle_ptr(const QMallocView& q, uint32_t h) 
     return (void*)(q.pool.base + (size_t)h * 16u);
 }
 
-// Carves one chunk of class `cls` for refill lane `ri` of `r_total` (b blocks
-// per chunk) and enqueues the blocks no refill lane takes; returns the
-// chunk's first page or -1.
-__device__ __forceinline__ int32_t q_carve(const QMallocView& q, int cls, uint32_t ri, uint32_t r_total, uint32_t b,
-                                           int32_t seed_own, uint32_t max_steps, int32_t* steps) {
+// Marks a claimed chunk (first page `chunk`) as class `cls`, for refill lane
+// `ri` of `r_total` (b blocks per chunk), and enqueues the blocks no refill
+// lane takes.
+__device__ __forceinline__ void q_carve_finish(const QMallocView& q, int cls, uint32_t ri, uint32_t r_total,
+                                               uint32_t b, int32_t chunk) {
     const uint32_t npages = q_chunk_bytes(q, cls) >> q.page_shift;
-    const int32_t chunk = walk_span(q.pool, npages, seed_own, max_steps, steps);
-    if (chunk < 0) return -1;
     q.class_of[(uint32_t)chunk] = (uint8_t)(cls + 1);
     for (uint32_t p = 1; p < npages; ++p) q.class_of[(uint32_t)chunk + p] = (uint8_t)(kQCont | (cls + 1));
     atomicAdd(q.counters + kQChunks, 1ull);
@@ -127,6 +125,16 @@ __device__ __forceinline__ int32_t q_carve(const QMallocView& q, int cls, uint32
     const uint32_t first = (uint32_t)(((size_t)(uint32_t)chunk << q.page_shift) >> 4);
     const uint32_t users = r_total - ri < b ? r_total - ri : b;   // refill lanes served by this chunk
     q_enqueue_run(q, cls, first + users * (bytes >> 4), bytes >> 4, b - users);
+}
+
+// Carves one chunk of class `cls` (walk, then q_carve_finish); returns the
+// chunk's first page or -1.
+__device__ __forceinline__ int32_t q_carve(const QMallocView& q, int cls, uint32_t ri, uint32_t r_total, uint32_t b,
+                                           int32_t seed_own, uint32_t max_steps, int32_t* steps) {
+    const uint32_t npages = q_chunk_bytes(q, cls) >> q.page_shift;
+    const int32_t chunk = walk_span(q.pool, npages, seed_own, max_steps, steps);
+    if (chunk < 0) return -1;
+    q_carve_finish(q, cls, ri, r_total, b, chunk);
     return chunk;
 }
 
@@ -182,6 +190,14 @@ __device__ __forceinline__ void* qmalloc_group(const QMallocView& q, uint32_t ac
             if (lane == l) chunk = q_carve(q, cls, ri, r_total, b, seed_own, max_steps, &steps);
             __syncwarp(active);
         }
+    } else if (active == kFull32) {
+        // the warp walks for all its chunks together (walk_span_warp); chunks
+        // of more than 32 pages walk on their own
+        const uint32_t npages = carver ? q_chunk_bytes(q, cls) >> q.page_shift : 0u;
+        chunk = walk_span_warp(q.pool, npages <= 32u ? npages : 0u, seed_own, max_steps, &steps);
+        if (npages > 32u) chunk = walk_span(q.pool, npages, seed_own, max_steps, &steps);
+        if (!carver) steps = 0;
+        if (chunk >= 0) q_carve_finish(q, cls, ri, r_total, b, chunk);
     } else if (carver) {
         chunk = q_carve(q, cls, ri, r_total, b, seed_own, max_steps, &steps);
     }

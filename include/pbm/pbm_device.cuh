@@ -786,6 +786,18 @@ __device__ __forceinline__ int32_t walk_span(const PoolView& v, uint32_t n, int3
     return -1;
 }
 
+// Affine jump-ahead of the LCG by lane + 1 steps: lcg31 applied lane + 1
+// times to x is (aj * x + cj) mod 2^31.  The same table serves every walk of
+// the warp, so it is computed once per call.
+__device__ __forceinline__ void lcg_jump_for_lane(uint32_t lane, uint32_t& aj, uint32_t& cj) {
+    aj = 1103515245u;
+    cj = 12345u;
+    for (uint32_t k = 0; k < lane; ++k) {
+        cj = 1103515245u * cj + 12345u;
+        aj *= 1103515245u;
+    }
+}
+
 // Runs of need_n <= 32 pages (0 = none) for the lanes of a whole warp, each
 // lane on its own LCG sequence from seed0; steps = jumps.  Every needing
 // lane first takes one jump of its own (all in parallel).  Each lane still
@@ -811,13 +823,9 @@ __device__ __forceinline__ int32_t walk_span_warp(const PoolView& v, uint32_t ne
         const int32_t f = span_in_pair(w, v0, v1, need_n, L);
         if (f >= 0 && claim_span(v, (uint32_t)f, need_n)) id = f;
     }
-    // this lane's jump ahead by lane + 1 LCG steps: x -> (aj * x + cj) mod 2^31
-    uint32_t aj = 1103515245u, cj = 12345u;
-    for (uint32_t k = 0; k < lane; ++k) {
-        cj = 1103515245u * cj + 12345u;
-        aj *= 1103515245u;
-    }
     uint32_t pend = __ballot_sync(kFull32, need_n > 0u && id < 0 && s < max_steps);
+    uint32_t aj = 0u, cj = 0u;                             // jump ahead by lane + 1 steps
+    if (pend) lcg_jump_for_lane(lane, aj, cj);
     while (pend) {
         const int l0 = __ffs((int)pend) - 1;
         const uint32_t x0 = (uint32_t)__shfl_sync(kFull32, x, l0);

@@ -223,18 +223,34 @@ __global__ void __launch_bounds__(256, MINB) k_batch_persistent(BatchArgs a, con
             slot = wrap_slot(gd.offset + (q - pre[g]), a.arena_len);
         };
         const unsigned long long q = q0 + lane;
-        const bool active = q < total;
+        bool active;
         int op = PBM_OP_ALLOC;
         unsigned long long slot = 0;
-        if (active) locate(q, op, slot);
         if constexpr (K == BWalk::Collab2) {
             const unsigned long long qb = q + 32ull;
-            const bool act_b = qb < total;
+            bool act_b;
             int op_b = PBM_OP_ALLOC;
             unsigned long long slot_b = 0;
-            if (act_b) locate(qb, op_b, slot_b);
+            if (q0 + CH <= g0_end) {
+                // the whole chunk lies in one group: its slots follow on from one base
+                const pbm_group gd = groups[g0];
+                const unsigned long long base = wrap_slot(gd.offset + (q0 - pre[g0]), a.arena_len);
+                slot = wrap_slot(base + lane, a.arena_len);
+                slot_b = wrap_slot(base + 32ull + lane, a.arena_len);
+                op = gd.op;
+                op_b = gd.op;
+                active = true;
+                act_b = true;
+            } else {
+                active = q < total;
+                act_b = qb < total;
+                if (active) locate(q, op, slot);
+                if (act_b) locate(qb, op_b, slot_b);
+            }
             batch_round2<Word>(a, seed, q0, active, op, slot, act_b, op_b, slot_b, lane_off, acc);
         } else {
+            active = q < total;
+            if (active) locate(q, op, slot);
             batch_round<K, W, Word>(a, seed, active, op, q, slot, lane_off, gslots, acc);
         }
     }

@@ -633,6 +633,47 @@ def config_occupancy_sweep(torch, pbm, stream, flush, rounds=16, N=1 << 22, max_
             "churn_note": "alloc+free swaps on the held pages (occupancy constant), batched graph form"}
 
 
+def config_strategies(torch, pbm, stream, flush, occs=(0.5, 0.9), n=1 << 20, reps=3):
+    """Every allocation strategy of the reference's device API (parallelPage.cuh:7-75,
+    the header-only walks) through pbm_alloc / pbm_free: a 2^24-page pool
+    prefilled to each occupancy (seed 2), 2^20 claims in one launch, then their
+    frees in one launch, L2 flushed before each; alloc+free ops/s (median of
+    the repetitions) and mean steps per claim."""
+    sh = stream.cuda_stream
+    strategies = [("RandomWalk", pbm.RANDOM_WALK), ("RandomWalk_BM", pbm.RANDOM_WALK_BM),
+                  ("CollabRW_BM", pbm.COLLAB_RW_BM), ("ClusteredRandomWalk_BM", pbm.CLUSTERED_RW_BM),
+                  ("LinkedList", pbm.LINKED_LIST), ("SingleClock", pbm.SINGLE_CLOCK), ("DistClock", pbm.DIST_CLOCK)]
+    ids = torch.empty(n, dtype=torch.int32, device="cuda")
+    steps = torch.empty(n, dtype=torch.int32, device="cuda")
+    out = {"pool_pages": T_PAGES, "requests_per_launch": n, "unit": "ops/s", "ops": "claims + frees",
+           "l2": "flushed before every launch", "by_occupancy": {}}
+    pool = pbm.Pool(T_PAGES, PAGE_SIZE)
+    for occ in occs:
+        res = {}
+        for name, strat in strategies:
+            cfg = pbm.walk_config(strat)
+            pool.reset(sh)
+            pool.prefill(occ, PREFILL_SEED, sh)
+            used0 = pool.used(sh)
+            pool.alloc(cfg, n, 11, ids, steps, stream=sh)       # untimed: builds the free list where one is used
+            pool.free(cfg, n, ids, stream=sh)
+            ms = []
+            for r in range(reps):
+                flush.zero_()
+                ta = _ev_ms(torch, stream, lambda: pool.alloc(cfg, n, 12 + r, ids, steps, stream=sh))
+                st = steps.cpu().numpy()
+                ok = int((ids.cpu().numpy() >= 0).sum())
+                flush.zero_()
+                tf = _ev_ms(torch, stream, lambda: pool.free(cfg, n, ids, stream=sh))
+                ms.append(ta + tf)
+            res[name] = {"value": 2 * n / (float(np.median(ms)) * 1e-3), "claims_ok": ok,
+                         "mean_steps": float(st[st > 0].mean()) if (st > 0).any() else 0.0,
+                         "occupancy_restored": pool.used(sh) == used0}
+        out["by_occupancy"][f"{int(occ * 100)}%"] = res
+    pool.close()
+    return out
+
+
 def config_buffer_manager(torch, pbm, stream, flush, n_fetch=1 << 26, round_size=1 << 18):
     """2^22 frames x 4 KiB over 2^24 logical pages; 2^26 fetches Zipf(0.99)
     over a seed-3 permutation; each pin held Geometric(0.25) rounds."""
@@ -813,6 +854,7 @@ def run_configs(args, torch, pbm, stream):
     todo = [("claim_write_free_50pct", lambda: config_claim_write_free(torch, pbm, stream,
                                                                       cpu=not args.no_cpu_baseline)),
             ("occupancy_sweep", lambda: config_occupancy_sweep(torch, pbm, stream, flush)),
+            ("strategies", lambda: config_strategies(torch, pbm, stream, flush)),
             ("buffer_manager", lambda: config_buffer_manager(torch, pbm, stream, flush)),
             ("malloc", lambda: config_malloc(torch, pbm, stream, flush)),
             ("serving", lambda: config_serving(torch, pbm, stream))]
@@ -1045,7 +1087,7 @@ def main():
                     help="a small case of another kernel, for ncu (alloc also runs the free kernel)")
     ap.add_argument("--configs", default="all",
                     help="other workloads measured after the headline: all, none, or a comma list of "
-                         "claim_write_free_50pct,occupancy_sweep,buffer_manager,malloc,serving")
+                         "claim_write_free_50pct,occupancy_sweep,strategies,buffer_manager,malloc,serving")
     args = ap.parse_args()
     rank, world, local_rank = env_rank()
     if args.profile:

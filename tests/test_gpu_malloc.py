@@ -131,3 +131,37 @@ def test_parallel_malloc_free_rounds(cuda, pbm_mod, orc, mode):
     assert live == 0 and bad == 0
     assert (ptrs.cpu().numpy() == 0).all()
     pool.close()
+
+
+@pytest.mark.parametrize("occ,seed", [(0.5, 8), (0.5, 9), (0.3, 3)])
+def test_one_request_warp_walk_matches_oracle(cuda, pbm_mod, orc, occ, seed):
+    """A batch of one 64 KiB request (a run of 16 pages): the request's lane
+    takes its first jump and then the whole warp walks for it, 32 jumps per
+    round.  With nothing else claiming, the run it gets is the one the
+    oracle's one-lane span walk finds from the same seed, and the bitmap
+    changes by exactly that run."""
+    torch = cuda
+    pbm = pbm_mod
+    T, S = 1 << 16, 77
+    pool = pbm.Pool(T, PAGE, materialize=True)
+    pool.prefill(occ, seed)
+    pool.malloc_init()
+    before = pool.read_bitmap()
+    exp_ids, _ = orc.replay_spans(before.copy(), T, np.array([16], dtype=np.int32), S, max_steps=4096)
+    d_sizes = torch.tensor([65536], dtype=torch.int32, device="cuda")
+    ptrs = torch.zeros(1, dtype=torch.int64, device="cuda")
+    tab = _tab([(pbm.OP_MALLOC, 1, 0)])
+    pool.malloc_batch(torch.from_numpy(tab.view(np.uint8).copy()).cuda(), None, 1, d_sizes, ptrs, 1, S,
+                      pbm.LAUNCH_PERSISTENT, max_steps=4096)
+    torch.cuda.synchronize()
+    p = int(ptrs.cpu().numpy()[0])
+    got = (p - pool.base_ptr) // PAGE if p else -1
+    assert got == int(exp_ids[0])
+    after = pool.read_bitmap()
+    bits_b = np.unpackbits(before.view(np.uint8), bitorder="little")[:T]
+    bits_a = np.unpackbits(after.view(np.uint8), bitorder="little")[:T]
+    if got >= 0:
+        assert (bits_a[got:got + 16] == 1).all() and (bits_b[got:got + 16] == 0).all()
+        bits_a[got:got + 16] = 0
+    assert np.array_equal(bits_a, bits_b)
+    pool.close()

@@ -18,6 +18,9 @@ Forms timed on the same requests:
            the timed region
 The L2 is flushed (512 MiB write) between timed steps, outside the events.
 
+Output: one JSON line per other workload ("detail" lines), then the headline
+as the last line of stdout, a compact object of at most HEADLINE_MAX_BYTES.
+
 `--impl reference` times the reference's algorithm on the host cores: the
 std::atomic replay of its word-probe walk (RandomWalkBasic_BM) over the same
 churn, all hardware threads (the reference ships no CPU implementation).  The
@@ -61,6 +64,72 @@ UNIT = "ops/s"
 # step of `bench.py --profile --profile-walk pair32c`), summarised in
 # profiles/batch_persistent_collab32_90pct.md.
 NCU_DRAM_BYTES_PER_PAIR = 7.815424e6 / 1420753
+
+
+HEADLINE_MAX_BYTES = 1400
+
+
+def _sig(x, digits=5):
+    """A float rounded to `digits` significant figures (keeps the headline short)."""
+    if isinstance(x, float) and math.isfinite(x) and x != 0.0:
+        return round(x, digits - 1 - int(math.floor(math.log10(abs(x)))))
+    return x
+
+
+def _short(d, digits=5):
+    if isinstance(d, dict):
+        return {k: _short(v, digits) for k, v in d.items()}
+    if isinstance(d, (list, tuple)):
+        return [_short(v, digits) for v in d]
+    return _sig(d, digits)
+
+
+# keys of the headline line, in print order; everything else is a detail line
+HEADLINE_KEYS = ("impl", "metric", "value", "unit", "n_gpus", "steps", "warmup", "ms_per_step", "higher_is_better",
+                 "scaling", "vs_baseline", "dtype", "data", "config", "e2e", "roofline", "cpu_baseline", "clocks",
+                 "gpu_launches", "plain_value", "batched_over_plain", "invariants_ok", "reference_cuda_build")
+SUB_KEYS = {
+    "config": ("workload", "walk", "l2", "launch"),
+    "e2e": ("value", "unit", "h2d_bytes_per_step", "d2h_bytes_per_step"),
+    "roofline": ("bound", "achieved", "peak", "unit", "frac", "traffic", "peak_source", "line_pattern_peak",
+                 "hbm_frac"),
+    "cpu_baseline": ("value", "unit", "cores", "kind", "sample"),
+    "clocks": ("sm_mhz", "sm_max_mhz", "reasons"),
+    "reference_cuda_build": ("collab_ops_s", "rwbasic_ops_s"),
+}
+
+
+def headline(full):
+    """The one JSON line printed last: the keys of HEADLINE_KEYS (nested
+    objects cut to SUB_KEYS), floats to five significant figures.  A log
+    reader that keeps only the end of stdout still sees the whole line; the
+    rest of the run's results go out as detail lines before it."""
+    out = {}
+    for k in HEADLINE_KEYS:
+        if k not in full:
+            continue
+        v = full[k]
+        if isinstance(v, dict) and k in SUB_KEYS:
+            v = {s: v[s] for s in SUB_KEYS[k] if s in v}
+        out[k] = _short(v)
+    s = json.dumps(out, separators=(",", ":"))
+    if len(s) > HEADLINE_MAX_BYTES:           # long free-text fields go first, never the numbers
+        for k, s2 in (("cpu_baseline", "sample"), ("config", "walk"), ("config", "workload")):
+            if k in out and isinstance(out[k], dict) and s2 in out[k] and len(s) > HEADLINE_MAX_BYTES:
+                out[k][s2] = str(out[k][s2])[:60]
+                s = json.dumps(out, separators=(",", ":"))
+    return s
+
+
+def emit(full, details, path=None):
+    """Detail lines first (one JSON object per workload, key "detail"), then
+    the headline.  `path`: also write everything as one JSON file."""
+    for name, obj in details.items():
+        print(json.dumps({"detail": name, **(obj if isinstance(obj, dict) else {"value": obj})}), flush=True)
+    if path:
+        with open(path, "w") as f:
+            json.dump({"headline": full, "details": details}, f, indent=1)
+    print(headline(full), flush=True)
 
 
 def env_rank():
@@ -212,9 +281,10 @@ def run_reference(args, rank):
         "data": "synthetic", "config": workload_config(),
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-        "reference_cuda_build": ref_gpu,
+        "reference_cuda_build": {w + "_ops_s": (ref_gpu.get(w) or {}).get("value")
+                                 for w in ("collab", "rwbasic")},
     }
-    print(json.dumps(line), flush=True)
+    emit(line, {"reference_cuda_build": ref_gpu}, args.details)
     return 0
 
 
@@ -359,9 +429,12 @@ def run_ours(args, rank, world, local_rank):
     g_ms, value = combine_ranks(g_ms, g_ops, world, dist, dev)
     st = pool.stats(sh)
 
-    # ---- plain: one launch per group ----
-    res_plain = timed(lambda s: pool.batch(cfg, None, h_groups(s), N_GROUPS, arena, H, SEED0 + s,
-                                           pbm.LAUNCH_PLAIN, stream=sh), range(args.warmup, min(n_steps, args.warmup + 100)))
+    # ---- plain: one launch per group (the ctypes group arrays are built
+    # before the timed region, so the events see only the launches) ----
+    plain_steps = range(args.warmup, min(n_steps, args.warmup + 100))
+    plain_groups = {s: h_groups(s) for s in plain_steps}
+    res_plain = timed(lambda s: pool.batch(cfg, None, plain_groups[s], N_GROUPS, arena, H, SEED0 + s,
+                                           pbm.LAUNCH_PLAIN, stream=sh), plain_steps)
     p_ms = sum(ms for _, ms in res_plain)
     plain_value = sum(2 * int(pairs_per_step[s]) for s, _ in res_plain) / (p_ms * 1e-3)
 
@@ -436,8 +509,9 @@ def run_ours(args, rank, world, local_rank):
     roofline = {
         "bound": "l2_atomic", "achieved": atomic_achieved / 1e9, "peak": ceil_ops / 1e9, "unit": "Gatomic/s",
         "frac": atomic_achieved / ceil_ops, "traffic": traffic,
-        "peak_source": "pbm_atomic_ceiling, spread pattern (uncontended atomicOr, 32 lanes on 32 lines), same run",
+        "peak_source": "spread-pattern atomicOr ceiling (32 lanes on 32 lines), same run",
         "line_pattern_peak": ceil_line / 1e9, "frac_of_line_pattern": atomic_achieved / ceil_line,
+        "hbm_frac": hbm_achieved / hbm_peak,
         "kernel": "k_batch_persistent of the tuned walk (see tuned_config): one launch per graph replay",
         "hbm": {"achieved": hbm_achieved, "peak": hbm_peak, "unit": "GB/s", "frac": hbm_achieved / hbm_peak,
                 "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)" if peaks else "fallback"},
@@ -451,7 +525,8 @@ def run_ours(args, rank, world, local_rank):
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": g_ms / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic",
-        "config": dict(workload_config(), walk=cfg_dict(cfg)),
+        "config": dict(workload_config(), walk="{walk}/{word_bits}b/w{width}/s{stride}/b{blocks_per_sm}".format(
+            **cfg_dict(cfg))),
         "plain_value": plain_value, "batched_over_plain": value / world / plain_value,
         "per_thread_walk_value": per_thread_value,
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(np.mean(e2e_bytes_in)),
@@ -474,10 +549,14 @@ def run_ours(args, rank, world, local_rank):
     g_pt.close()
     pool.close()
     del flush
+    details = {"headline_full": {k: line[k] for k in ("roofline", "e2e", "cpu_baseline", "clocks", "tuned_config",
+                                                      "autotune_top", "atomic_ceiling_ops_s", "per_thread_walk_value",
+                                                      "collab_mean_steps", "failures", "mean_pairs_per_step",
+                                                      "wall_s_timed_region")}}
     if rank == 0 and world == 1:
-        line["configs"] = run_configs(args, torch, pbm, stream)
+        details.update(run_configs(args, torch, pbm, stream))
     if rank == 0:
-        print(json.dumps(line), flush=True)
+        emit(line, details, args.details)
     if dist:
         dist.barrier()
         dist.destroy_process_group()
@@ -1088,6 +1167,8 @@ def main():
     ap.add_argument("--configs", default="all",
                     help="other workloads measured after the headline: all, none, or a comma list of "
                          "claim_write_free_50pct,occupancy_sweep,strategies,buffer_manager,malloc,serving")
+    ap.add_argument("--details", default=None,
+                    help="also write the headline and every workload's results as one JSON file here")
     args = ap.parse_args()
     rank, world, local_rank = env_rank()
     if args.profile:

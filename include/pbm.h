@@ -461,16 +461,18 @@ int pbm_check_ids(pbm_pool *pool, const int32_t *d_ids, uint32_t n, pbm_check_re
 
 /* The same invariant check for callers that cannot allocate device memory
  * (no counterpart in the reference).  An engine that gives all of its device
- * memory to its own buffer pool at start-up, or code that runs while stream
- * capture forbids cudaMalloc, has the bitmap and the id list already but no
- * way to get scratch.  This entry point calls no cudaMalloc/cudaFree: its
- * scratch (one bit per page plus counters) is a static device array of
+ * memory to its own buffer pool at start-up, or a process that must not grow
+ * its device footprint after start-up, has the bitmap and the id list already
+ * but no way to get scratch.  This entry point calls no cudaMalloc/cudaFree:
+ * its scratch (one bit per page plus counters) is a static device array of
  * 1 MiB + 128 B that every GPU loading libpbm.so keeps until exit, so it
- * accepts at most 8,388,608 pages (PBM_ERR_INVALID beyond).  d_bitmap uses
- * the pool layout (bit p of 32-bit word p/32 = page p held).  All calls share
- * the scratch: calls that overlap on the GPU race, so serialise them.  The
- * first call on a device resolves the scratch address (cudaGetSymbolAddress),
- * so make it before any stream capture. */
+ * accepts at most 8,388,608 pages and INT32_MAX ids (PBM_ERR_INVALID beyond).
+ * d_bitmap uses the pool layout (bit p of 32-bit word p/32 = page p held).
+ * All calls share the scratch and each call clears it first: calls that
+ * overlap on the GPU race, so serialise them.  The call waits for `stream`
+ * before it returns.  The first call on a device (and again after a device
+ * reset) resolves the scratch address (cudaGetSymbolAddress), so make it
+ * before any stream capture. */
 int pbm_check_ids_noalloc(const uint32_t *d_bitmap, uint64_t n_pages, const int32_t *d_ids,
                           uint32_t n, pbm_check_result *h_out, void *stream);
 

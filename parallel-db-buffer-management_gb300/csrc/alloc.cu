@@ -44,10 +44,10 @@ enum class Walk { Page, Word32, Word64, Crw, SingleClock, DistClock };
 template <Walk K>
 __global__ void __launch_bounds__(256) k_alloc_thread(AllocArgs a) {
     Acc acc;
-    const uint32_t tid = blockIdx.x * blockDim.x + threadIdx.x;
-    const uint32_t nthr = gridDim.x * blockDim.x;
-    const uint32_t n_round = (a.n + 31u) & ~31u;
-    for (uint32_t r = tid; r < n_round; r += nthr) {
+    const uint64_t tid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const uint64_t nthr = (uint64_t)gridDim.x * blockDim.x;
+    const uint64_t n_round = ((uint64_t)a.n + 31u) & ~31ull;
+    for (uint64_t r = tid; r < n_round; r += nthr) {
         if (r >= a.n) continue;
         int32_t s = 0, id = -1;
         const int32_t seed0 = request_seed(a.seed, r);
@@ -86,15 +86,15 @@ template <int W, typename Word>
 __global__ void __launch_bounds__(256) k_alloc_collab(AllocArgs a) {
     __shared__ int32_t slots[256];
     Acc acc;
-    const uint32_t tid = blockIdx.x * blockDim.x + threadIdx.x;
-    const uint32_t nthr = gridDim.x * blockDim.x;
+    const uint64_t tid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const uint64_t nthr = (uint64_t)gridDim.x * blockDim.x;
     const uint32_t gl = threadIdx.x & (uint32_t)(W - 1);
     const uint32_t L = WordTraits<Word>::count(a.v);
     const uint32_t lane_off = (uint32_t)(((unsigned long long)gl * a.stride) % L);
     volatile int32_t* my_slots = slots + (threadIdx.x & ~(uint32_t)(W - 1));
     // trip count uniform across each group of W lanes
-    for (uint32_t base = tid - gl; base < a.n; base += nthr) {
-        const uint32_t r = base + gl;
+    for (uint64_t base = tid - gl; base < a.n; base += nthr) {
+        const uint64_t r = base + gl;
         const bool need = r < a.n;
         int32_t s = 0;
         int32_t id = walk_collab<W, Word>(a.v, need, request_seed(a.seed, base), lane_off,
@@ -112,9 +112,9 @@ __global__ void __launch_bounds__(256) k_alloc_collab(AllocArgs a) {
 
 __global__ void __launch_bounds__(256) k_fifo_alloc(AllocArgs a, FifoState* st, int32_t* ring) {
     Acc acc;
-    const uint32_t tid = blockIdx.x * blockDim.x + threadIdx.x;
-    const uint32_t nthr = gridDim.x * blockDim.x;
-    for (uint32_t r = tid; r < a.n; r += nthr) {
+    const uint64_t tid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const uint64_t nthr = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t r = tid; r < a.n; r += nthr) {
         int32_t s = 0;
         int32_t id = fifo_get(a.v, st, ring, a.stats, &s);
         a.ids[r] = id;
@@ -129,7 +129,7 @@ __global__ void __launch_bounds__(256) k_fifo_alloc(AllocArgs a, FifoState* st, 
 __global__ void __launch_bounds__(256) k_fifo_free(PoolView v, uint32_t n, const int32_t* ids,
                                                    FifoState* st, int32_t* ring, DevStats* stats) {
     unsigned long long f = 0;
-    for (uint32_t r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x) {
+    for (uint64_t r = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; r < n; r += (uint64_t)gridDim.x * blockDim.x) {
         int32_t id = ids[r];
         if (id < 0 || (uint32_t)id >= v.n_pages) continue;
         if (fifo_put(v, st, ring, stats, id)) ++f;
@@ -141,10 +141,10 @@ __global__ void __launch_bounds__(256) k_fifo_free(PoolView v, uint32_t n, const
 __global__ void __launch_bounds__(256) k_free_pages(PoolView v, uint32_t n, const int32_t* ids,
                                                     int merge, DevStats* stats) {
     unsigned long long f = 0;
-    const uint32_t tid = blockIdx.x * blockDim.x + threadIdx.x;
-    const uint32_t nthr = gridDim.x * blockDim.x;
-    const uint32_t n_round = (n + 31u) & ~31u;
-    for (uint32_t r = tid; r < n_round; r += nthr) {
+    const uint64_t tid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const uint64_t nthr = (uint64_t)gridDim.x * blockDim.x;
+    const uint64_t n_round = ((uint64_t)n + 31u) & ~31ull;
+    for (uint64_t r = tid; r < n_round; r += nthr) {
         int32_t id = r < n ? ids[r] : -1;
         if (id >= (int32_t)v.n_pages) id = -1;
         if (merge && blockDim.x >= 32) {
@@ -163,7 +163,7 @@ __global__ void __launch_bounds__(256) k_free_pages(PoolView v, uint32_t n, cons
 template <bool SPAN>
 __global__ void __launch_bounds__(256) k_alloc_runs(AllocArgs a, const int32_t* npages) {
     Acc acc;
-    for (uint32_t r = blockIdx.x * blockDim.x + threadIdx.x; r < a.n; r += gridDim.x * blockDim.x) {
+    for (uint64_t r = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; r < a.n; r += (uint64_t)gridDim.x * blockDim.x) {
         int32_t k = npages[r];
         int32_t s = 0, id = -1;
         if (SPAN) {
@@ -184,7 +184,7 @@ __global__ void __launch_bounds__(256) k_alloc_runs(AllocArgs a, const int32_t* 
 __global__ void __launch_bounds__(256) k_free_runs(PoolView v, uint32_t n, const int32_t* ids,
                                                    const int32_t* npages, DevStats* stats) {
     unsigned long long f = 0;
-    for (uint32_t r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x) {
+    for (uint64_t r = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; r < n; r += (uint64_t)gridDim.x * blockDim.x) {
         int32_t id = ids[r], k = npages[r];
         if (id < 0 || k < 1 || (uint32_t)k > kMaxSpanPages || (unsigned long long)id + (uint32_t)k > v.n_pages)
             continue;
@@ -202,7 +202,7 @@ __global__ void __launch_bounds__(256) k_free_runs(PoolView v, uint32_t n, const
 __global__ void __launch_bounds__(256) k_claim_write_free(AllocArgs a, uint32_t payload_words, int hold) {
     Acc acc;
     unsigned long long frees = 0;
-    for (uint32_t r = blockIdx.x * blockDim.x + threadIdx.x; r < a.n; r += gridDim.x * blockDim.x) {
+    for (uint64_t r = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; r < a.n; r += (uint64_t)gridDim.x * blockDim.x) {
         int32_t s = 0;
         int32_t id = walk_page(a.v, request_seed(a.seed, r), a.max_steps, &s);
         a.ids[r] = id;

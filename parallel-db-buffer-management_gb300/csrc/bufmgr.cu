@@ -316,8 +316,8 @@ __global__ void __launch_bounds__(256) k_round(BmView b, const int32_t* release_
                                                const int32_t* release_idx, uint32_t n_release,
                                                const int32_t* pages, uint32_t n, uint32_t slot0,
                                                int32_t* frames_out) {
-    const uint32_t tid = blockIdx.x * blockDim.x + threadIdx.x;
-    const uint32_t nthr = gridDim.x * blockDim.x;
+    const uint64_t tid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const uint64_t nthr = (uint64_t)gridDim.x * blockDim.x;
     unsigned long long ok = 0, bad = 0;
     if (nthr == 1u) {
         for (uint32_t j = 0; j < n_release; ++j) unpin_k(b, release_frames_of[release_idx[j]], 1u, ok, bad);
@@ -325,8 +325,8 @@ __global__ void __launch_bounds__(256) k_round(BmView b, const int32_t* release_
         // warp-uniform trip count: lanes releasing pins of the same frame (hot
         // pages of a skewed stream) merge them into one atomic
         const uint32_t lane = threadIdx.x & 31u;
-        for (uint32_t base = tid - lane; base < n_release; base += nthr) {
-            const uint32_t j = base + lane;
+        for (uint64_t base = tid - lane; base < n_release; base += nthr) {
+            const uint64_t j = base + lane;
             const int32_t f = j < n_release ? release_frames_of[release_idx[j]] : -1;
             const bool valid = f >= 0 && (uint32_t)f < b.n_frames;
             const uint32_t peers = __match_any_sync(0xffffffffu, valid ? (uint32_t)f : 0x80000000u + lane);
@@ -346,8 +346,8 @@ __global__ void __launch_bounds__(256) k_round(BmView b, const int32_t* release_
         // warp-uniform trip count (blockDim is a multiple of 32), so the warp
         // can merge the pins of lanes fetching the same page
         const uint32_t lane = threadIdx.x & 31u;
-        for (uint32_t base = tid - lane; base < n; base += nthr) {
-            const uint32_t i = base + lane;
+        for (uint64_t base = tid - lane; base < n; base += nthr) {
+            const uint64_t i = base + lane;
             const int32_t p = i < n ? pages[i] : -1;
             const bool valid = p >= 0 && (uint32_t)p < b.n_logical;
             const uint32_t key = valid ? (uint32_t)p : 0x80000000u + lane;   // invalid lanes never merge
@@ -382,7 +382,7 @@ __global__ void __launch_bounds__(256) k_round(BmView b, const int32_t* release_
                 f = hit;
                 ++acc.hits;
             } else if (valid && !loader) {
-                f = fetch<DIST>(b, (uint32_t)p, (slot0 + i) % b.n_arms, kHandBatch, acc);
+                f = fetch<DIST>(b, (uint32_t)p, (slot0 + (uint32_t)i) % b.n_arms, kHandBatch, acc);
             }
             if (i < n) frames_out[i] = f;
         }
@@ -393,14 +393,14 @@ __global__ void __launch_bounds__(256) k_round(BmView b, const int32_t* release_
 }
 
 __global__ void k_bm_init(BmView b) {
-    const uint32_t tid = blockIdx.x * blockDim.x + threadIdx.x;
-    const uint32_t nthr = gridDim.x * blockDim.x;
-    for (uint32_t p = tid; p < b.n_logical; p += nthr) b.page_table[p] = -1;
-    for (uint32_t f = tid; f < b.n_frames; f += nthr) {
+    const uint64_t tid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const uint64_t nthr = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t p = tid; p < b.n_logical; p += nthr) b.page_table[p] = -1;
+    for (uint64_t f = tid; f < b.n_frames; f += nthr) {
         b.frame_state[f] = (unsigned long long)kEmptyPage << 32;
         b.ref[f] = 0;
     }
-    for (uint32_t a = tid; a < b.n_arms; a += nthr)
+    for (uint64_t a = tid; a < b.n_arms; a += nthr)
         b.arms[a] = (uint32_t)(((unsigned long long)a * b.n_frames) / b.n_arms);
     if (tid == 0) *b.single_hand = 0ull;
 }
@@ -411,17 +411,17 @@ struct BmCheck {
 };
 
 __global__ void k_bm_check(BmView b, BmCheck* out) {
-    const uint32_t tid = blockIdx.x * blockDim.x + threadIdx.x;
-    const uint32_t nthr = gridDim.x * blockDim.x;
+    const uint64_t tid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const uint64_t nthr = (uint64_t)gridDim.x * blockDim.x;
     unsigned long long res = 0, mapped = 0, mism = 0, loading = 0, pins = 0;
-    for (uint32_t p = tid; p < b.n_logical; p += nthr) {
+    for (uint64_t p = tid; p < b.n_logical; p += nthr) {
         int32_t f = b.page_table[p];
         if (f == kLoading) { ++loading; continue; }
         if (f < 0) continue;
         ++res;
         if ((uint32_t)f >= b.n_frames || (uint32_t)(b.frame_state[f] >> 32) != p) ++mism;
     }
-    for (uint32_t f = tid; f < b.n_frames; f += nthr) {
+    for (uint64_t f = tid; f < b.n_frames; f += nthr) {
         unsigned long long s = b.frame_state[f];
         uint32_t pg = (uint32_t)(s >> 32);
         pins += (uint32_t)s;

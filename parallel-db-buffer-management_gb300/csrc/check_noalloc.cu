@@ -4,22 +4,27 @@
 // handed to two requesters, plus a few counters.  It takes that scratch from
 // its pool, which was set up with cudaMalloc.  Some callers cannot call
 // cudaMalloc at all: a database engine that hands every byte of device
-// memory to its own buffer pool up front, code running while a stream
-// capture forbids allocation, or a process that must not grow its device
-// footprint after start-up.  For them, pbm_check_ids_noalloc works on
-// buffers the caller already has (the bitmap and the id list) and keeps its
-// scratch in the static array below, which exists once per GPU that loads
-// this library and stays allocated until the process exits.
+// memory to its own buffer pool up front, or a process that must not grow
+// its device footprint after start-up (a cudaMalloc there either fails or
+// takes memory the engine has already promised elsewhere).  For them,
+// pbm_check_ids_noalloc works on buffers the caller already has (the bitmap
+// and the id list) and keeps its scratch in the static array below, which
+// exists once per GPU that loads this library and stays allocated until the
+// process exits.
 //
 // Limits and sharing rules:
 //   * at most kNoAllocMaxPages pages (8,388,608 pages: 1 MiB of seen bits);
-//     larger pools are rejected with PBM_ERR_INVALID;
+//     larger pools are rejected with PBM_ERR_INVALID, and so are id lists
+//     longer than INT32_MAX (ids are int32 page numbers);
 //   * every call uses the same scratch array.  Each call clears it before use,
 //     but two calls whose work overlaps on the GPU (different streams, or
 //     different host threads) race on it and give wrong counts: serialise them;
-//   * the first call on a device looks up the array's device address with
-//     cudaGetSymbolAddress (a set-up step that is not a stream operation), so
-//     make that first call before any stream capture starts.
+//   * the call waits for its stream before it returns (it reads the counters
+//     back to the host);
+//   * the first call on a device (in each CUDA context of that device) looks
+//     up the array's device address with cudaGetSymbolAddress, a set-up step
+//     that is not a stream operation, so make that first call before any
+//     stream capture starts.
 #include <mutex>
 
 #include "internal.cuh"
@@ -40,17 +45,52 @@ struct Counters {
 };
 
 std::mutex g_setup_mu;
-uint32_t* g_scratch_ptr[kMaxDevices] = {};
+struct ScratchSlot {
+    unsigned long long ctx_id;   // the context the address belongs to (0: not looked up yet)
+    uint32_t* ptr;
+};
+ScratchSlot g_scratch[kMaxDevices] = {};
 
-// Device address of the scratch on the current device; looked up once per
-// device with that device current.  Host code must not use the symbol
-// g_noalloc_scratch itself as an address: on the host it is a stand-in.
+// Identity of the current CUDA context, from the driver's cuCtxGetCurrent and
+// cuCtxGetId (reached through the runtime's entry-point query, so the library
+// does not link libcuda).  A device reset makes a new context with a new id,
+// and the array's address is then looked up again.  Returns 0 if unknown.
+unsigned long long current_context_id() {
+    using GetCurrent = int (*)(void**);
+    using GetId = int (*)(void*, unsigned long long*);
+    static GetCurrent get_current = nullptr;
+    static GetId get_id = nullptr;
+    static bool tried = false;
+    if (!tried) {
+        tried = true;
+        cudaDriverEntryPointQueryResult q1, q2;
+        void* f1 = nullptr;
+        void* f2 = nullptr;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f1, 12000, cudaEnableDefault, &q1) == cudaSuccess &&
+            cudaGetDriverEntryPointByVersion("cuCtxGetId", &f2, 12000, cudaEnableDefault, &q2) == cudaSuccess &&
+            q1 == cudaDriverEntryPointSuccess && q2 == cudaDriverEntryPointSuccess) {
+            get_current = (GetCurrent)f1;
+            get_id = (GetId)f2;
+        }
+        cudaGetLastError();
+    }
+    void* ctx = nullptr;
+    unsigned long long id = 0;
+    if (!get_current || !get_id || get_current(&ctx) != 0 || !ctx || get_id(ctx, &id) != 0) return 0;
+    return id;
+}
+
+// Device address of the scratch on the current device, looked up once per
+// device and context with that device current.  Host code must not use the
+// symbol g_noalloc_scratch itself as an address: on the host it is a stand-in.
 int scratch_address(uint32_t** out) {
     int dev = 0;
     PBM_CUDA_TRY(cudaGetDevice(&dev));
     if (dev < 0 || dev >= kMaxDevices) return PBM_ERR_INVALID;
+    const unsigned long long ctx = current_context_id();   // 0 before the context exists
     std::lock_guard<std::mutex> lk(g_setup_mu);
-    if (!g_scratch_ptr[dev]) {
+    ScratchSlot& slot = g_scratch[dev];
+    if (!slot.ptr || ctx == 0 || slot.ctx_id != ctx) {
         void* p = nullptr;
         cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
         if (e != cudaSuccess || !p) {
@@ -59,9 +99,10 @@ int scratch_address(uint32_t** out) {
             cudaGetLastError();
             return PBM_ERR_CUDA;
         }
-        g_scratch_ptr[dev] = (uint32_t*)p;
+        slot.ptr = (uint32_t*)p;
+        slot.ctx_id = current_context_id();   // the lookup has made the context current
     }
-    *out = g_scratch_ptr[dev];
+    *out = slot.ptr;
     return PBM_OK;
 }
 
@@ -75,8 +116,8 @@ __global__ void __launch_bounds__(256) k_noalloc_check(const uint32_t* words, ui
                                                        const int32_t* ids, uint32_t n, uint32_t* seen,
                                                        Counters* out) {
     unsigned long long ok = 0, failed = 0, oor = 0, dup = 0, unmarked = 0;
-    const uint32_t n_round = (n + 31u) & ~31u;
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n_round; i += gridDim.x * blockDim.x) {
+    const uint64_t n_round = ((uint64_t)n + 31u) & ~31ull;
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n_round; i += (uint64_t)gridDim.x * blockDim.x) {
         if (i >= n) continue;
         int32_t id = ids[i];
         if (id == -1) { ++failed; continue; }
@@ -106,8 +147,8 @@ __global__ void __launch_bounds__(256) k_noalloc_used(const uint32_t* words, uin
     const uint32_t tail = (uint32_t)(n_pages % 32u);
     unsigned long long c = 0;
     const uint32_t total = full + (tail ? 1u : 0u);
-    const uint32_t n_round = (total + 31u) & ~31u;
-    for (uint32_t w = blockIdx.x * blockDim.x + threadIdx.x; w < n_round; w += gridDim.x * blockDim.x) {
+    const uint64_t n_round = ((uint64_t)total + 31u) & ~31ull;
+    for (uint64_t w = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; w < n_round; w += (uint64_t)gridDim.x * blockDim.x) {
         if (w >= total) continue;
         uint32_t v = __ldcg(words + w);
         if (w == full) v &= (1u << tail) - 1u;
@@ -125,6 +166,10 @@ using namespace pbm;
 extern "C" int pbm_check_ids_noalloc(const uint32_t* d_bitmap, uint64_t n_pages, const int32_t* d_ids,
                                      uint32_t n, pbm_check_result* h_out, void* stream) {
     if (!d_bitmap || !h_out || (n && !d_ids) || n_pages == 0) return PBM_ERR_INVALID;
+    if (n > (uint32_t)INT32_MAX) {
+        std::fprintf(stderr, "[pbm] pbm_check_ids_noalloc: %u ids exceed INT32_MAX\n", n);
+        return PBM_ERR_INVALID;
+    }
     if (n_pages > kNoAllocMaxPages) {
         std::fprintf(stderr,
                      "[pbm] pbm_check_ids_noalloc: %llu pages exceed the no-alloc limit of %llu pages\n",

@@ -135,7 +135,7 @@ __global__ void __launch_bounds__(256) k_malloc_plain(MArgs a) {
 }
 
 __global__ void k_malloc_init(int32_t* start_of, int32_t* live, uint8_t* len_of, uint32_t n) {
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
         start_of[i] = -1;
         live[i] = 0;
         len_of[i] = 0;

@@ -30,7 +30,7 @@ struct HostBlock {
 __global__ void __launch_bounds__(256) k_monitor_popcount(const unsigned long long* words, uint32_t n_words64,
                                                           unsigned long long* out) {
     unsigned long long c = 0;
-    for (uint32_t w = blockIdx.x * blockDim.x + threadIdx.x; w < n_words64; w += gridDim.x * blockDim.x)
+    for (uint64_t w = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; w < n_words64; w += (uint64_t)gridDim.x * blockDim.x)
         c += (unsigned long long)__popcll(__ldcg(words + w));
     pbm::block_add_counters<1>({c}, {out});
 }

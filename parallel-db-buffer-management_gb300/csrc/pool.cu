@@ -47,8 +47,8 @@ bool device_writable(const void* p) {
 // Bernoulli(occ) bitmap: one thread per 32-bit word, one hash per page.
 __global__ void k_prefill(uint32_t* words, uint32_t n_words, uint64_t n_pages,
                           uint64_t thresh53, uint64_t seed) {
-    for (uint32_t w = blockIdx.x * blockDim.x + threadIdx.x; w < n_words;
-         w += gridDim.x * blockDim.x) {
+    for (uint64_t w = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; w < n_words;
+         w += (uint64_t)gridDim.x * blockDim.x) {
         uint32_t val = 0;
         uint64_t p0 = (uint64_t)w * 32u;
 #pragma unroll 8
@@ -63,8 +63,8 @@ __global__ void k_prefill(uint32_t* words, uint32_t n_words, uint64_t n_pages,
 
 // Padding bits only (reset): clear every word, then set bits >= n_pages.
 __global__ void k_reset_words(uint32_t* words, uint32_t n_words, uint64_t n_pages) {
-    for (uint32_t w = blockIdx.x * blockDim.x + threadIdx.x; w < n_words;
-         w += gridDim.x * blockDim.x) {
+    for (uint64_t w = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; w < n_words;
+         w += (uint64_t)gridDim.x * blockDim.x) {
         uint64_t p0 = (uint64_t)w * 32u;
         uint32_t val = 0;
         if (p0 + 32u > n_pages) {
@@ -111,8 +111,8 @@ __device__ __forceinline__ unsigned long long block_sum(unsigned long long v) {
 __global__ void k_popcount(const unsigned long long* words, uint32_t n_words64,
                            unsigned long long* out) {
     unsigned long long c = 0;
-    for (uint32_t w = blockIdx.x * blockDim.x + threadIdx.x; w < n_words64;
-         w += gridDim.x * blockDim.x)
+    for (uint64_t w = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; w < n_words64;
+         w += (uint64_t)gridDim.x * blockDim.x)
         c += (unsigned long long)__popcll(__ldcg(words + w));
     c = block_sum(c);
     if (threadIdx.x == 0 && c) atomicAdd(out, c);
@@ -123,7 +123,7 @@ __global__ void k_popcount(const unsigned long long* words, uint32_t n_words64,
 __global__ void k_check_ids(const uint32_t* words, uint32_t* seen, uint64_t n_pages,
                             const int32_t* ids, uint32_t n, CheckCounters* out) {
     unsigned long long ok = 0, failed = 0, oor = 0, dup = 0, unmarked = 0;
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
         int32_t id = ids[i];
         if (id == -1) { ++failed; continue; }
         if (id < 0 || (uint64_t)id >= n_pages) { ++oor; continue; }
@@ -275,7 +275,7 @@ static void pool_free_all(pbm_pool* p) {
 }
 
 __global__ void k_init_slots(int32_t* cursors, uint32_t* arms, uint32_t max_slots, uint32_t n_pages) {
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < max_slots; i += gridDim.x * blockDim.x) {
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < max_slots; i += (uint64_t)gridDim.x * blockDim.x) {
         cursors[i] = -1;
         // distributed clock: arm0 = idx(lcg(seed(0, slot)), T) (parallelPage.cu:546-555 randomises arms)
         arms[i] = idx_hi(lcg(request_seed(0u, i)), n_pages);

@@ -625,10 +625,14 @@ def config_occupancy_sweep(torch, pbm, stream, flush, rounds=16, N=1 << 22, max_
     pool = pbm.Pool(T_PAGES, PAGE_SIZE, materialize=True)
     ids = torch.empty(N, dtype=torch.int32, device="cuda")
     steps = torch.empty(N, dtype=torch.int32, device="cuda")
+    # fail fast: a popcount pass before each launch sets its budget of free
+    # pages, and the requests past it fail at once instead of walking
+    # max_steps jumps (the pass is inside the timed launch)
     walks = {
-        "collab32": pbm.walk_config(pbm.COLLAB_RW_BM, word_bits=32, collab_width=32, max_steps=max_steps),
-        "word_probe32": pbm.walk_config(pbm.RANDOM_WALK_BM, word_bits=32, max_steps=max_steps),
-        "page_probe": pbm.walk_config(pbm.RANDOM_WALK, max_steps=max_steps),
+        "collab32": pbm.walk_config(pbm.COLLAB_RW_BM, word_bits=32, collab_width=32, max_steps=max_steps,
+                                    fail_fast=1),
+        "word_probe32": pbm.walk_config(pbm.RANDOM_WALK_BM, word_bits=32, max_steps=max_steps, fail_fast=1),
+        "page_probe": pbm.walk_config(pbm.RANDOM_WALK, max_steps=max_steps, fail_fast=1),
     }
     gen = torch.Generator(device="cuda")
     res = {}
@@ -707,6 +711,7 @@ def config_occupancy_sweep(torch, pbm, stream, flush, rounds=16, N=1 << 22, max_
     pool.close()
     return {"rounds": rounds, "requests_per_launch": N, "max_steps": max_steps, "unit": "ops/s",
             "ops": "get-page requests issued + pages freed", "l2": "flushed before every launch",
+            "fail_fast": "requests past the free pages counted before each launch fail at once",
             "by_occupancy": res, "autotune_by_band": tuned,
             "churn_by_occupancy_ops_s": churn,
             "churn_note": "alloc+free swaps on the held pages (occupancy constant), batched graph form"}
@@ -889,7 +894,10 @@ def config_serving(torch, pbm, stream, rates=(1e5, 1e6, 1e7, 1e8, 1e9, 1e10, 1e1
                    horizon_s=1.0):
     """64 tenants, Poisson arrivals at an aggregate page rate, batches
     LogU[1,65536] pages, mix 45% alloc / 45% free / 10% Zipf(0.99) fetch,
-    seed 5; 2^24-page pool prefilled to 80%, budget 95%.  The rates past
+    seed 5; 2^24-page pool prefilled to 80%, shared budget up to 95%: an
+    ALLOC that does not fit waits for frees (p50/p99 include the wait;
+    `over_budget` counts only ALLOCs larger than the whole budget, `stranded`
+    the requests still waiting when nothing more could run).  The rates past
     1e9 (the workload's range) look for the loop's capacity: where the wall
     time exceeds the arrival span, throughput is the saturation rate and the
     latencies include queueing."""
@@ -921,7 +929,7 @@ def config_serving(torch, pbm, stream, rates=(1e5, 1e6, 1e7, 1e8, 1e9, 1e10, 1e1
             "throughput": rep.pages / rep.wall_s, "p50_ms": rep.p50_s * 1e3, "p99_ms": rep.p99_s * 1e3,
             "batches": rep.batches, "mean_batch_requests": rep.mean_batch_requests,
             "max_in_flight": rep.max_in_flight, "over_budget": int((st == pbm.ERR_EXHAUSTED).sum()),
-            "rc": rc}
+            "waited_for_memory": int(rep.waited), "stranded": int(rep.stranded), "rc": rc}
         srv.close()
         bm.close()
         pool.close()

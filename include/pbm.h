@@ -79,6 +79,12 @@ typedef struct {
     int32_t  blocks_per_sm; /* persistent form: resident blocks per SM (0 = occupancy limit;
                                >= 5 selects the register-capped kernels, 5 blocks) */
     int32_t  free_merge;    /* 1 = merge frees of one word within a warp */
+    int32_t  fail_fast;     /* pbm_alloc: 1 = count the free pages F before the launch (a pass over
+                               the bitmap); requests r >= F fail at once instead of walking to
+                               max_steps, the others walk as usual -- or, when the launch asks for
+                               at least half of the F pages, request r takes the r-th free page in
+                               ascending order (one atomic, no walk) */
+    int32_t  reserved;
 } pbm_walk_config;
 
 /* One caller's group in a batch.  Requests of the batch are numbered in
@@ -365,6 +371,13 @@ int pbm_bufmgr_round(pbm_bufmgr *m, const int32_t *d_frames_of, const int32_t *d
 int pbm_bufmgr_stats(pbm_bufmgr *m, pbm_bufmgr_counters *h_out, void *stream);
 int pbm_bufmgr_check(pbm_bufmgr *m, pbm_bufmgr_check_result *h_out, void *stream);
 int pbm_bufmgr_frames(pbm_bufmgr *m, void **d_frames, size_t *bytes);
+/* Copies the maps to the host (either pointer may be NULL; synchronises
+ * `stream`): h_page_entries[n_logical], one 64-bit word per logical page --
+ * the frame holding it in the high 32 bits (signed: -1 not resident, -2 and
+ * -3 a load in progress), the CLOCK reference bit in bit 31, its pins in
+ * bits 0..30; h_frame_pages[n_frames], the page each frame holds
+ * (0xffffffff empty).  No reference counterpart. */
+int pbm_bufmgr_read_tables(pbm_bufmgr *m, uint64_t *h_page_entries, uint32_t *h_frame_pages, void *stream);
 /* Copies the first bytes_per_frame bytes of each listed frame into d_out
  * (ids < 0 give zeros). */
 int pbm_bufmgr_gather(pbm_bufmgr *m, const int32_t *d_frame_ids, uint32_t n, uint32_t bytes_per_frame,
@@ -377,16 +390,20 @@ int pbm_bufmgr_gather(pbm_bufmgr *m, const int32_t *d_frame_ids, uint32_t n, uin
  * ALLOC n: n new pages appended to the tenant's ring of page slots.
  * FREE n:  releases min(n, pages the tenant holds) of its oldest pages.
  * FETCH n: pins then releases the next n pages of the shared fetch trace.
- * A tenant's requests are admitted in arrival order.  Admission is by
- * free-page budget: each tenant may hold at most tenant_quota_pages (0 = the
- * pages free below max_occupancy at create time, split evenly), and an ALLOC
- * that would exceed it is rejected (status PBM_ERR_EXHAUSTED) -- only the
- * tenant's own later FREEs could make room, and they queue behind it.  A
- * FREE waits until the pages it releases are allocated on the device.
- * Admitted requests of all tenants form the next batch whenever one of
- * n_streams batch slots is free, so batches overlap on the device.  Page
- * counts and statuses per request depend only on the tenant's own requests
- * and quota (results do not depend on the mix). */
+ * Admission is by a free-page budget shared by all tenants: the pages free
+ * below max_occupancy at create time.  An ALLOC that does not fit the budget
+ * now waits until frees land (frees count once their batch has finished);
+ * only an ALLOC larger than the budget, the tenant's ring or its optional
+ * quota is rejected (status PBM_ERR_EXHAUSTED).  A tenant's ALLOCs keep
+ * their arrival order; a later FREE may pass a waiting ALLOC when all the
+ * pages it releases are older than that ALLOC, a FETCH always may.  A FREE
+ * waits until the pages it releases are allocated on the device.  Admitted
+ * requests of all tenants form the next batch whenever one of n_streams
+ * batch slots is free, so batches overlap on the device.  A request's status
+ * and page count depend only on its tenant's own requests, so they are the
+ * same alone and in a mix for every request the mix admits; when nothing is
+ * left to arrive or run and nothing more can be admitted, the run stops and
+ * the requests still waiting end with status -1 (counted as stranded). */
 #define PBM_REQ_ALLOC 0
 #define PBM_REQ_FREE  1
 #define PBM_REQ_FETCH 2
@@ -412,8 +429,8 @@ typedef struct {
     uint32_t n_streams;           /* batches in flight at most */
     uint32_t max_batch_requests;  /* requests per batch at most (<= 2048) */
     uint32_t max_fetch_pages;     /* fetch pages per batch at most (0 = 1<<22) */
-    uint32_t tenant_quota_pages;  /* pages a tenant may hold (0 = even split, see above) */
-    double   max_occupancy;       /* bound on held pages / pool pages (sets the default quota) */
+    uint32_t tenant_quota_pages;  /* pages one tenant may hold (0 = no cap beyond the shared budget) */
+    double   max_occupancy;       /* bound on held pages / pool pages (sets the shared budget) */
     double   drain_timeout_s;     /* stop waiting this long after the last arrival */
     pbm_walk_config walk;         /* allocation walk of the batches */
 } pbm_server_config;
@@ -421,6 +438,8 @@ typedef struct {
 typedef struct {
     uint64_t requests, completed, rejected, pages, batches, max_in_flight;
     double   wall_s, p50_s, p99_s, mean_batch_requests;
+    uint64_t waited;      /* ALLOCs that waited for memory before admission */
+    uint64_t stranded;    /* requests still waiting when the run stopped (status -1) */
 } pbm_server_report;
 
 typedef struct pbm_server pbm_server;

@@ -47,11 +47,11 @@ struct HostState {
 };
 
 inline bool create_pool(uint64_t n_pages, uint32_t page_size, uint32_t max_slots, bool build_fifo,
-                        HostState* hs, DeviceState* ds) {
+                        HostState* hs, DeviceState* ds, bool with_pages = true) {
     pbm_pool_config c{};
     c.n_pages = n_pages;
     c.page_size = page_size;
-    c.flags = PBM_POOL_MATERIALIZE;
+    c.flags = with_pages ? PBM_POOL_MATERIALIZE : 0u;
     c.max_slots = max_slots;
     int rc = pbm_pool_create(&c, &hs->pool);
     if (rc != PBM_OK) {

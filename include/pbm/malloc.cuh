@@ -7,8 +7,8 @@
 // two, 2 KiB .. 64 KiB; the reference's 264-byte pages cannot hold its own
 // 64 KiB-class chunks).  Differences from the reference, by design: free()
 // releases memory (KernelMallocSimple::free is empty in the reference,
-// malloc.cu:194-196, and KernelMallocCollab frees only whole chunks,
-// malloc.cu:337-357); the destructor leaves the pool alive because kernel
+// malloc.cu:157-159, and KernelMallocCollab frees only whole chunks,
+// malloc.cu:300-320); the destructor leaves the pool alive because kernel
 // arguments are copies of the object -- call release() to free it.
 #pragma once
 #include <climits>
@@ -25,7 +25,7 @@
 
 class MemoryManager {
 public:
-    /* MemoryManager(maxNThreads): malloc.cu:52-56 */
+    /* MemoryManager(maxNThreads): malloc.cuh:6, malloc.cu:15-19 */
     __host__ MemoryManager(int _maxNThreads = INT_MAX) : m_maxNThreads(_maxNThreads) {
         pbm_pool_config c{};
         c.n_pages = PBM_MALLOC_POOL_PAGES;
@@ -53,7 +53,7 @@ public:
         m_view.page_shift = sh;
     }
     __host__ ~MemoryManager() {}
-    /* reset(): free all memory (malloc.cu:118-123, 250-253) */
+    /* reset(): free all memory (malloc.cu:82-86, 214-216) */
     __host__ void reset() {
         if (!m_pool) return;
         pbm_malloc_release(m_pool);
@@ -93,13 +93,13 @@ public:
     pbm_pool* m_pool;
 };
 
-/* KernelMallocSimple(maxNThreads): malloc.cu:98-197 */
+/* KernelMallocSimple(maxNThreads): malloc.cuh:14-24, malloc.cu:61-160 */
 class KernelMallocSimple : public MemoryManager {
 public:
     __host__ KernelMallocSimple(int _maxNThreads) : MemoryManager(_maxNThreads) {}
 };
 
-/* KernelMallocCollab(): malloc.cu:238-358 */
+/* KernelMallocCollab(): malloc.cuh:27-37, malloc.cu:201-320 */
 class KernelMallocCollab : public MemoryManager {
 public:
     __host__ KernelMallocCollab() : MemoryManager() {}

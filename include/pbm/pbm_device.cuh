@@ -945,6 +945,35 @@ __device__ __forceinline__ void free_page_warp(const PoolView& v, uint32_t activ
     if (id >= 0 && (__ffs((int)peers) - 1) == (int)lane) atomicAnd(v.words + w, ~merged);
 }
 
+// ---------------------------------------------------------------------------
+// Launch budget: fail fast in an exhausted pool.  A pass over the bitmap just
+// before the launch counts the free pages F.  Request r of the launch may
+// take a page only if r < F: the requests past the pages that were free
+// fail at once instead of walking to their step bound, and no more pages are
+// granted than were free at the start -- with no atomic at all, so the
+// launch never contends on a shared counter.  When the launch asks for at
+// least half of the F free pages (`list_mode`), the pass also lists the free
+// pages in ascending order, and request r takes list[r] directly instead of
+// searching for it.  A null budget grants every request.
+// ---------------------------------------------------------------------------
+struct LaunchBudget {
+    long long free_at_start;    // F
+    int32_t list_mode;          // 1: list[0..F) holds the free pages in order
+    int32_t pad;
+};
+
+__device__ __forceinline__ bool budget_grants(const LaunchBudget* b, unsigned long long r) {
+    return !b || (long long)r < __ldcg(&b->free_at_start);
+}
+
+// A listed page, claimed with one atomicOr; -1 if another claim (a launch on
+// another stream) took it first.
+__device__ __forceinline__ int32_t take_listed(const PoolView& v, const int32_t* list, long long index) {
+    const int32_t p = __ldcg(list + index);
+    const uint32_t bit = 1u << ((uint32_t)p & 31u);
+    return (atomicOr(v.words + ((uint32_t)p >> 5), bit) & bit) ? -1 : p;
+}
+
 __device__ __forceinline__ void* page_address(const PoolView& v, int32_t id) {
     return (void*)(v.base + (size_t)(uint32_t)id * v.page_size);
 }

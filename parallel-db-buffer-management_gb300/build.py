@@ -17,6 +17,10 @@ CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "lib")
 OBJ_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "libpbm.so")
+# the -rdc link form of the parallelPage.cuh drop-in (a static library of
+# relocatable device code that a caller links with -rdc=true)
+DROPIN_SRC = os.path.join(HERE, "dropin", "parallelPage_lib.cu")
+DROPIN_LIB = os.path.join(OUT_DIR, "libpbm_dropin.a")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + [
@@ -79,6 +83,10 @@ def build(force: bool = False, verbose: bool = False) -> str:
     if force or jobs or _stale(LIB, objs):
         cmd = [nvcc, "-shared", "-o", LIB] + objs + ARCH + ["-Xcompiler", "-fPIC"]
         run(cmd)
+    if force or _stale(DROPIN_LIB, [DROPIN_SRC] + hdrs):
+        obj = os.path.join(OBJ_DIR, "parallelPage_lib.o")
+        run([nvcc, "-rdc=true", "-c", DROPIN_SRC, "-o", obj] + NVCC_FLAGS)
+        run([nvcc, "-lib", "-o", DROPIN_LIB, obj] + ARCH)
     return LIB
 
 

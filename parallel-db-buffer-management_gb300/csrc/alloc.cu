@@ -26,6 +26,8 @@ struct AllocArgs {
     unsigned long long* arm;     // single clock
     uint32_t max_slots;
     int32_t dedupe;              // collaborative walk: W*stride may exceed L
+    LaunchBudget* budget;        // fail-fast launch budget (null: every request walks)
+    const int32_t* free_list;    // the budget's list of free pages (list mode)
 };
 
 // Per-thread accumulators reduced once per block.
@@ -47,17 +49,31 @@ __global__ void __launch_bounds__(256) k_alloc_thread(AllocArgs a) {
     const uint64_t tid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
     const uint64_t nthr = (uint64_t)gridDim.x * blockDim.x;
     const uint64_t n_round = ((uint64_t)a.n + 31u) & ~31ull;
+    // whole warps iterate together (n_round and nthr are multiples of 32), or
+    // one thread in the serial replay
+    const bool listed = a.budget && __ldcg(&a.budget->list_mode);
     for (uint64_t r = tid; r < n_round; r += nthr) {
-        if (r >= a.n) continue;
+        const bool go = r < a.n && budget_grants(a.budget, r);
         int32_t s = 0, id = -1;
-        const int32_t seed0 = request_seed(a.seed, r);
-        if constexpr (K == Walk::Page) {
+        if (go && listed) {
+            id = take_listed(a.v, a.free_list, (long long)r);   // request r takes the r-th free page
+            s = 1;
+        }
+        if (r >= a.n || id >= 0) {
+            // past the last request, or served from the list
+        } else if (!go) {
+            // past the launch budget: no free page is left for this request
+        } else if constexpr (K == Walk::Page) {
+            const int32_t seed0 = request_seed(a.seed, r);
             id = walk_page(a.v, seed0, a.max_steps, &s);
         } else if constexpr (K == Walk::Word32) {
+            const int32_t seed0 = request_seed(a.seed, r);
             id = walk_word<uint32_t>(a.v, seed0, a.max_steps, &s);
         } else if constexpr (K == Walk::Word64) {
+            const int32_t seed0 = request_seed(a.seed, r);
             id = walk_word<uint64_t>(a.v, seed0, a.max_steps, &s);
         } else if constexpr (K == Walk::Crw) {
+            const int32_t seed0 = request_seed(a.seed, r);
             int32_t* cur = a.cursors + (r % a.max_slots);
             int32_t c = *cur;
             id = walk_crw(a.v, &c, seed0, a.max_steps, &s);
@@ -70,6 +86,7 @@ __global__ void __launch_bounds__(256) k_alloc_thread(AllocArgs a) {
             id = sweep_dist(a.v, &ar, a.max_steps, &s);
             *arm = ar;
         }
+        if (r >= a.n) continue;
         a.ids[r] = id;
         if (a.steps) a.steps[r] = s;
         acc.ok += id >= 0;
@@ -92,16 +109,22 @@ __global__ void __launch_bounds__(256) k_alloc_collab(AllocArgs a) {
     const uint32_t L = WordTraits<Word>::count(a.v);
     const uint32_t lane_off = (uint32_t)(((unsigned long long)gl * a.stride) % L);
     volatile int32_t* my_slots = slots + (threadIdx.x & ~(uint32_t)(W - 1));
+    const bool listed = a.budget && __ldcg(&a.budget->list_mode);
     // trip count uniform across each group of W lanes
     for (uint64_t base = tid - gl; base < a.n; base += nthr) {
         const uint64_t r = base + gl;
-        const bool need = r < a.n;
+        const bool need = r < a.n && budget_grants(a.budget, r);
+        const int32_t from_list = (need && listed) ? take_listed(a.v, a.free_list, (long long)r) : -1;
         int32_t s = 0;
-        int32_t id = walk_collab<W, Word>(a.v, need, request_seed(a.seed, base), lane_off,
+        int32_t id = walk_collab<W, Word>(a.v, need && from_list < 0, request_seed(a.seed, base), lane_off,
                                           a.dedupe != 0, a.max_steps, my_slots, &s);
-        if (need) {
+        if (from_list >= 0) {
+            id = from_list;
+            s = 1;
+        }
+        if (r < a.n) {
             a.ids[r] = id;
-            if (a.steps) a.steps[r] = s;
+            if (a.steps) a.steps[r] = need ? s : 0;   // refused by the budget: no walk
             acc.ok += id >= 0;
             acc.fail += id < 0;
             acc.steps += (unsigned long long)s;
@@ -267,6 +290,8 @@ AllocArgs make_args(pbm_pool* p, const pbm_walk_config* c, uint32_t n, uint32_t 
     int W = c->collab_width ? c->collab_width : 32;
     uint32_t L = c->word_bits == 64 ? p->view.n_words64 : p->view.n_words32;
     a.dedupe = ((unsigned long long)(W - 1) * a.stride >= L) ? 1 : 0;
+    a.budget = nullptr;
+    a.free_list = nullptr;
     return a;
 }
 
@@ -331,17 +356,25 @@ extern "C" {
 
 int pbm_alloc(pbm_pool* pool, const pbm_walk_config* cfg, uint32_t n, uint32_t seed, int32_t* d_ids,
               int32_t* d_steps, void* stream) {
+    PBM_ON_POOL_DEVICE(pool);
     if (!pool || (n && !d_ids)) return PBM_ERR_INVALID;
     int rc = check_cfg(cfg);
     if (rc) return rc;
     if (n == 0) return PBM_OK;
     AllocArgs a = make_args(pool, cfg, n, seed, d_ids, d_steps);
     if (cfg->strategy != PBM_LINKED_LIST) pool->fifo_valid = false;
+    if (cfg->fail_fast && cfg->strategy != PBM_LINKED_LIST) {   // the free list counts its pages itself
+        rc = budget_prepare(pool, n, (cudaStream_t)stream);
+        if (rc) return rc;
+        a.budget = pool->d_budget;
+        a.free_list = pool->d_free_list;
+    }
     return launch_alloc(pool, cfg, a, false, (cudaStream_t)stream);
 }
 
 int pbm_alloc_serial(pbm_pool* pool, const pbm_walk_config* cfg, uint32_t n, uint32_t seed,
                      int32_t* d_ids, int32_t* d_steps, void* stream) {
+    PBM_ON_POOL_DEVICE(pool);
     if (!pool || (n && !d_ids)) return PBM_ERR_INVALID;
     int rc = check_cfg(cfg);
     if (rc) return rc;
@@ -352,6 +385,7 @@ int pbm_alloc_serial(pbm_pool* pool, const pbm_walk_config* cfg, uint32_t n, uin
 }
 
 int pbm_free(pbm_pool* pool, const pbm_walk_config* cfg, uint32_t n, const int32_t* d_ids, void* stream) {
+    PBM_ON_POOL_DEVICE(pool);
     if (!pool || (n && !d_ids)) return PBM_ERR_INVALID;
     int rc = check_cfg(cfg);
     if (rc) return rc;
@@ -393,25 +427,30 @@ static int alloc_runs_impl(pbm_pool* pool, uint32_t n, const int32_t* d_npages, 
 
 int pbm_alloc_runs(pbm_pool* pool, uint32_t n, const int32_t* d_npages, uint32_t seed,
                    uint32_t max_steps, int32_t* d_ids, int32_t* d_steps, void* stream) {
+    PBM_ON_POOL_DEVICE(pool);
     return alloc_runs_impl(pool, n, d_npages, seed, max_steps, d_ids, d_steps, false, false, stream);
 }
 
 int pbm_alloc_runs_serial(pbm_pool* pool, uint32_t n, const int32_t* d_npages, uint32_t seed,
                           uint32_t max_steps, int32_t* d_ids, int32_t* d_steps, void* stream) {
+    PBM_ON_POOL_DEVICE(pool);
     return alloc_runs_impl(pool, n, d_npages, seed, max_steps, d_ids, d_steps, true, false, stream);
 }
 
 int pbm_alloc_spans(pbm_pool* pool, uint32_t n, const int32_t* d_npages, uint32_t seed,
                     uint32_t max_steps, int32_t* d_ids, int32_t* d_steps, void* stream) {
+    PBM_ON_POOL_DEVICE(pool);
     return alloc_runs_impl(pool, n, d_npages, seed, max_steps, d_ids, d_steps, false, true, stream);
 }
 
 int pbm_alloc_spans_serial(pbm_pool* pool, uint32_t n, const int32_t* d_npages, uint32_t seed,
                            uint32_t max_steps, int32_t* d_ids, int32_t* d_steps, void* stream) {
+    PBM_ON_POOL_DEVICE(pool);
     return alloc_runs_impl(pool, n, d_npages, seed, max_steps, d_ids, d_steps, true, true, stream);
 }
 
 int pbm_free_runs(pbm_pool* pool, uint32_t n, const int32_t* d_ids, const int32_t* d_npages, void* stream) {
+    PBM_ON_POOL_DEVICE(pool);
     if (!pool || (n && (!d_ids || !d_npages))) return PBM_ERR_INVALID;
     if (n == 0) return PBM_OK;
     int grid = (int)((n + 255u) / 256u);
@@ -423,6 +462,7 @@ int pbm_free_runs(pbm_pool* pool, uint32_t n, const int32_t* d_ids, const int32_
 
 int pbm_claim_write_free(pbm_pool* pool, uint32_t n, uint32_t seed, uint32_t payload_bytes, int hold,
                          uint32_t max_steps, int32_t* d_ids, int32_t* d_steps, void* stream) {
+    PBM_ON_POOL_DEVICE(pool);
     if (!pool || (n && !d_ids) || !pool->d_base || payload_bytes > pool->page_size || (payload_bytes & 3u))
         return PBM_ERR_INVALID;
     if (n == 0) return PBM_OK;
@@ -439,6 +479,7 @@ int pbm_claim_write_free(pbm_pool* pool, uint32_t n, uint32_t seed, uint32_t pay
 
 int pbm_gather_pages(pbm_pool* pool, const int32_t* d_ids, uint32_t n, uint32_t bytes_per_page,
                      int32_t* d_out, void* stream) {
+    PBM_ON_POOL_DEVICE(pool);
     if (!pool || !pool->d_base || (n && (!d_ids || !d_out)) || bytes_per_page > pool->page_size ||
         (bytes_per_page & 3u) || bytes_per_page == 0)
         return PBM_ERR_INVALID;

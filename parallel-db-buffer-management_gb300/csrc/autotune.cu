@@ -74,6 +74,7 @@ std::vector<pbm_walk_config> candidates(uint32_t max_steps) {
 extern "C" int pbm_autotune(pbm_pool* pool, const pbm_group* d_groups, uint32_t n_groups, uint64_t requests,
                             int32_t* d_arena, uint64_t arena_len, uint32_t seed, int reps, uint32_t max_steps,
                             pbm_tune_result* h_out, uint32_t max_out, uint32_t* h_n_out, void* stream) {
+    PBM_ON_POOL_DEVICE(pool);
     if (!pool || !d_groups || !n_groups || !d_arena || !arena_len || reps < 1 || !h_out || !max_out || !h_n_out)
         return PBM_ERR_INVALID;
     cudaStream_t s = (cudaStream_t)stream;

@@ -459,6 +459,7 @@ extern "C" {
 int pbm_batch_launch_results(pbm_pool* pool, const pbm_walk_config* cfg, const pbm_group* d_groups,
                              const pbm_group* h_groups, uint32_t n_groups, int32_t* d_arena, uint64_t arena_len,
                              uint32_t seed, int32_t* d_steps, int32_t* results, int mode, void* stream) {
+    PBM_ON_POOL_DEVICE(pool);
     if (!pool || !d_arena || arena_len == 0) return PBM_ERR_INVALID;
     int rc = valid_cfg(cfg);
     if (rc) return rc;
@@ -532,6 +533,7 @@ int pbm_batch_launch_results(pbm_pool* pool, const pbm_walk_config* cfg, const p
 int pbm_batch_launch(pbm_pool* pool, const pbm_walk_config* cfg, const pbm_group* d_groups,
                      const pbm_group* h_groups, uint32_t n_groups, int32_t* d_arena,
                      uint64_t arena_len, uint32_t seed, int32_t* d_steps, int mode, void* stream) {
+    PBM_ON_POOL_DEVICE(pool);
     return pbm_batch_launch_results(pool, cfg, d_groups, h_groups, n_groups, d_arena, arena_len, seed, d_steps,
                                     nullptr, mode, stream);
 }
@@ -539,6 +541,7 @@ int pbm_batch_launch(pbm_pool* pool, const pbm_walk_config* cfg, const pbm_group
 int pbm_batch_graph_create(pbm_pool* pool, const pbm_walk_config* cfg, const pbm_group* d_groups,
                            uint32_t n_groups, uint32_t n_steps, int32_t* d_arena, uint64_t arena_len,
                            uint32_t seed0, void* stream, pbm_graph** out) {
+    PBM_ON_POOL_DEVICE(pool);
     return pbm_batch_graph_create_results(pool, cfg, d_groups, n_groups, n_steps, d_arena, arena_len, seed0, nullptr,
                                           stream, out);
 }
@@ -546,6 +549,7 @@ int pbm_batch_graph_create(pbm_pool* pool, const pbm_walk_config* cfg, const pbm
 int pbm_batch_graph_create_results(pbm_pool* pool, const pbm_walk_config* cfg, const pbm_group* d_groups,
                                    uint32_t n_groups, uint32_t n_steps, int32_t* d_arena, uint64_t arena_len,
                                    uint32_t seed0, int32_t* results, void* stream, pbm_graph** out) {
+    PBM_ON_POOL_DEVICE(pool);
     if (!pool || !d_groups || !d_arena || !out || n_groups == 0 || n_steps == 0 || arena_len == 0)
         return PBM_ERR_INVALID;
     if (results && !device_writable(results)) return PBM_ERR_INVALID;
@@ -554,6 +558,7 @@ int pbm_batch_graph_create_results(pbm_pool* pool, const pbm_walk_config* cfg, c
     *out = nullptr;
     cudaStream_t s = (cudaStream_t)stream;
     pbm_graph* g = new pbm_graph();
+    g->device = pool->device;
     g->graph = nullptr;
     g->exec = nullptr;
     g->d_step = nullptr;
@@ -632,6 +637,7 @@ int pbm_batch_graph_create_results(pbm_pool* pool, const pbm_walk_config* cfg, c
 
 int pbm_graph_replay(pbm_graph* g, void* stream) {
     if (!g || !g->exec) return PBM_ERR_INVALID;
+    pbm::DeviceScope scope(g->device);
     PBM_CUDA_TRY(cudaGraphLaunch(g->exec, (cudaStream_t)stream));
     count_launch(g->launches_per_replay);
     return PBM_OK;
@@ -639,6 +645,7 @@ int pbm_graph_replay(pbm_graph* g, void* stream) {
 
 int pbm_graph_set_step(pbm_graph* g, uint32_t step, void* stream) {
     if (!g) return PBM_ERR_INVALID;
+    pbm::DeviceScope scope(g->device);
     PBM_CUDA_TRY(cudaMemcpyAsync(g->d_step, &step, sizeof(step), cudaMemcpyHostToDevice, (cudaStream_t)stream));
     PBM_CUDA_TRY(cudaStreamSynchronize((cudaStream_t)stream));
     return PBM_OK;
@@ -646,6 +653,7 @@ int pbm_graph_set_step(pbm_graph* g, uint32_t step, void* stream) {
 
 int pbm_graph_destroy(pbm_graph* g) {
     if (!g) return PBM_ERR_INVALID;
+    pbm::DeviceScope scope(g->device);
     if (g->exec) cudaGraphExecDestroy(g->exec);
     if (g->graph) cudaGraphDestroy(g->graph);
     cudaFree(g->d_step);

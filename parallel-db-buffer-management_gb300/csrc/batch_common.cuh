@@ -95,4 +95,5 @@ struct pbm_graph {
     uint32_t* d_done;                 // blocks finished in the current replay
     unsigned long long* d_prefix;
     unsigned long long launches_per_replay;
+    int device;                       // the pool's device: replays run there
 };

@@ -3,29 +3,33 @@
 // The reference has page allocators only; its SingleClock / DistClock arms
 // sweep the free map (parallelPage.cu:491-509, 571-592) but there is no page
 // table, no reference bits and no eviction.  This file defines the buffer
-// manager on those sweep mechanics:
+// manager on those sweep mechanics.  Its state, laid out so that a hit
+// touches one 32-byte sector:
 //
-//   page_table[p]   frame holding logical page p, -1 not resident, -2 being
-//                   loaded by another request
-//   frame_state[f]  (page << 32) | pins in one 64-bit word.  A fetch pins with
-//                   one atomicAdd and keeps the pin only if the word it added
-//                   to still named its page (else it subtracts it again), so
-//                   hot frames see no compare-and-swap retries; a sweep takes
-//                   a frame only if it is unpinned and unchanged (one CAS), so
-//                   a pin in flight makes the sweep pass the frame by
-//   ref[f]          CLOCK reference bit, set on every fetch
-//   arms            SINGLE: one shared hand (atomicAdd); DIST: per-slot hands,
-//                   each starting at its own frame and advancing privately
+//   pt[p]          one 64-bit word per logical page: the frame holding p in
+//                  the high 32 bits (-1 not resident, -2 being loaded, -3 a
+//                  load that failed and is being left), the CLOCK reference
+//                  bit in bit 31 and the page's pins in bits 0..30
+//   frame_page[f]  the page frame f holds (0xffffffff: empty)
+//   hands          SINGLE: one shared hand (atomicAdd); DIST: per-slot hands,
+//                  each starting at its own frame and advancing privately
 //
-// fetch(p): resident -> pin it, set ref (hit).  Not resident -> become its
-// loader (CAS page_table -1 -> -2), sweep: skip pinned frames, clear the
-// reference bit of referenced ones (second chance), take the first unpinned
-// unreferenced frame, unmap its old page (eviction), optionally copy the
-// page from the backing store, map p (miss).  A fetch that finds no frame
-// within max_sweep hand steps fails (-1) instead of spinning; waits on a
-// loading page are bounded too.  Lanes of a warp that fetch the same page
-// pin it with one atomicAdd of their count (Zipf streams repeat hot pages
-// within a warp).
+// fetch(p) for k requests of p (the lanes of a warp that fetch one page
+// merge into one atomic): add k pins to pt[p] with one atomicAdd.  Resident
+// -> a hit; the reference bit is set with a second atomic only if it was
+// clear.  Not resident and no pins before -> this request loads the page:
+// it marks the entry loading, sweeps -- frames whose page is pinned are
+// passed, referenced ones lose their bit (second chance), the first
+// unpinned unreferenced frame is taken by a compare-and-swap of its page's
+// entry to not-resident (eviction) -- optionally copies the page from the
+// backing store, and publishes the frame (one miss; its k-1 companions are
+// hits).  Otherwise another request is loading it: the pins are already
+// counted, so the request waits (bounded) for the frame.  A load that finds
+// no frame within max_sweep hand steps fails all its k requests; requests
+// waiting on it leave (the last one out clears the failure) and try again,
+// where a second failure is final.  Releases unpin through frame_page.
+// One thread running the rounds in order reproduces the single-thread
+// replay of these semantics exactly.
 #include <cstring>
 #include <new>
 
@@ -35,17 +39,28 @@ namespace pbm {
 namespace {
 
 constexpr uint32_t kEmptyPage = 0xffffffffu;
+constexpr int32_t kNotResident = -1;
 constexpr int32_t kLoading = -2;
-constexpr uint32_t kFetchSpinLimit = 1u << 16;
+constexpr int32_t kFailed = -3;
+constexpr unsigned long long kFrameUnit = 1ull << 32;
+constexpr unsigned long long kRef = 1ull << 31;
+constexpr uint32_t kPinMask = 0x7fffffffu;
+constexpr unsigned long long kEntryNotResident = (unsigned long long)(uint32_t)kNotResident << 32;
+constexpr unsigned long long kEntryFailed = (unsigned long long)(uint32_t)kFailed << 32;
+constexpr uint32_t kFetchSpinLimit = 1u << 16;   // polls of a page another request is loading
+constexpr uint32_t kFetchAttempts = 1024u;        // fetches retried after a failed load
+
+__device__ __forceinline__ int32_t e_frame(unsigned long long e) { return (int32_t)(e >> 32); }
+__device__ __forceinline__ uint32_t e_pins(unsigned long long e) { return (uint32_t)e & kPinMask; }
+__device__ __forceinline__ bool e_ref(unsigned long long e) { return (e & kRef) != 0ull; }
 
 struct BmStats {
     unsigned long long hits, misses, evictions, failures, unpins, bad_unpins, timeouts, pad;
 };
 
 struct BmView {
-    int32_t* page_table;
-    unsigned long long* frame_state;
-    uint8_t* ref;
+    unsigned long long* pt;  // n_logical entries
+    uint32_t* frame_page;    // n_frames
     unsigned long long* single_hand;
     uint32_t* arms;
     const char* backing;     // n_logical * frame_size bytes, may be null
@@ -59,20 +74,50 @@ struct BmView {
     int32_t dist;            // 0 = single hand, 1 = per-slot hands
 };
 
-// Shared-hand positions a sweeping thread takes per atomic in parallel rounds.
-// Measured on the Zipf(0.99) trace: 8 raised fetches/s by 20% but dropped the
-// hit rate from 85.2% to 82.1% (positions reserved past the victim are
-// skipped, so the hand laps faster than frames are examined) and slowed the
-// 4 KiB-copy form by 37%; 2 kept the hit rate and gained nothing.  So the
-// hand moves one position per atomic, as the reference's SingleClock arm.
-constexpr uint32_t kHandBatch = 1;
+struct BmAcc {
+    unsigned long long hits = 0, misses = 0, evictions = 0, failures = 0, timeouts = 0;
+};
+
+// Frame f as a victim for `page`: empty frames are taken by writing their
+// page; a mapped frame is taken by turning its page's entry from (f, no
+// reference, no pins) to not resident.  `e` is the entry read for frame f's
+// page q (unused for empty frames).  Returns true if this thread took f.
+__device__ __forceinline__ bool take_frame(const BmView& b, uint32_t f, uint32_t q, unsigned long long e,
+                                           uint32_t page, uint32_t* old_page) {
+    if (q == kEmptyPage) {
+        if (atomicCAS(b.frame_page + f, kEmptyPage, page) != kEmptyPage) return false;
+        *old_page = kEmptyPage;
+        return true;
+    }
+    if (atomicCAS(b.pt + q, e, kEntryNotResident) != e) return false;
+    b.frame_page[f] = page;
+    *old_page = q;
+    return true;
+}
+
+// One frame under the hand: 0 pass, 1 candidate (q, e filled in).  A
+// referenced frame loses its reference bit here (second chance).
+__device__ __forceinline__ int examine(const BmView& b, uint32_t f, uint32_t* q_out, unsigned long long* e_out) {
+    const uint32_t q = __ldcg(b.frame_page + f);
+    *q_out = q;
+    if (q == kEmptyPage) return 1;
+    if (q >= b.n_logical) return 0;
+    const unsigned long long e = __ldcg(b.pt + q);
+    *e_out = e;
+    if (e_frame(e) != (int32_t)f || e_pins(e) != 0u) return 0;   // pinned, or changing hands
+    if (e_ref(e)) {
+        atomicAnd(b.pt + q, ~kRef);
+        return 0;
+    }
+    return 1;
+}
 
 // Per-slot hand (DistClock, parallelPage.cu:571-592): the slot's hand is
-// private, so it reads the next kLookahead frames' words and reference bits
-// in one round trip and then examines them in hand order exactly as the
-// one-step sweep does, stopping at the victim (the hand ends just past it,
-// and frames beyond it are untouched).  Never more frames at once than the
-// pool has, so one batch never sees a frame twice.
+// private, so it reads the next kLookahead frames' pages in one round trip
+// and then examines them in hand order exactly as the one-step sweep does,
+// stopping at the victim (the hand ends just past it, and frames beyond it
+// are untouched).  Never more frames at once than the pool has, so one
+// batch never sees a frame twice.
 constexpr uint32_t kLookahead = 8;
 
 __device__ __forceinline__ int32_t sweep_private(const BmView& b, uint32_t page, uint32_t slot,
@@ -82,134 +127,159 @@ __device__ __forceinline__ int32_t sweep_private(const BmView& b, uint32_t page,
     const uint32_t width = b.n_frames < kLookahead ? b.n_frames : kLookahead;
     int32_t out = -1;
     for (uint32_t done = 0; done < b.max_sweep && out < 0;) {
-        unsigned long long st[kLookahead];
-        uint8_t rf[kLookahead];
+        uint32_t qs[kLookahead];
 #pragma unroll
         for (uint32_t j = 0; j < kLookahead; ++j) {
             if (j < width) {
                 uint32_t f = arm + j;
                 if (f >= b.n_frames) f -= b.n_frames;
-                st[j] = __ldcg(b.frame_state + f);
-                rf[j] = b.ref[f];
+                qs[j] = __ldcg(b.frame_page + f);
             }
         }
+        unsigned long long es[kLookahead];
+#pragma unroll
+        for (uint32_t j = 0; j < kLookahead; ++j)
+            es[j] = (j < width && qs[j] < b.n_logical) ? __ldcg(b.pt + qs[j]) : 0ull;
 #pragma unroll
         for (uint32_t j = 0; j < kLookahead; ++j) {
             if (j >= width || done >= b.max_sweep || out >= 0) break;
             const uint32_t f = arm;
             arm = f + 1u == b.n_frames ? 0u : f + 1u;
             ++done;
-            if ((uint32_t)st[j] != 0u) continue;                // pinned
-            if (rf[j]) { b.ref[f] = 0; continue; }              // second chance
-            const unsigned long long ns = ((unsigned long long)page << 32) | 1ull;
-            if (atomicCAS(b.frame_state + f, st[j], ns) == st[j]) {
-                *old_page = (uint32_t)(st[j] >> 32);
-                out = (int32_t)f;
+            const uint32_t q = qs[j];
+            const unsigned long long e = es[j];
+            if (q != kEmptyPage) {
+                if (q >= b.n_logical || e_frame(e) != (int32_t)f || e_pins(e) != 0u) continue;
+                if (e_ref(e)) { atomicAnd(b.pt + q, ~kRef); continue; }   // second chance
             }
+            if (take_frame(b, f, q, e, page, old_page)) out = (int32_t)f;
         }
     }
     b.arms[slot] = arm;
     return out;
 }
 
-// Victim search; returns a frame now holding (page, 1 pin) and its old page.
-// The shared hand advances `batch` positions per atomic, which the sweeping
-// thread then examines in order (parallelPage.cu:491-509 steps it by one).
+// Victim search of one thread; returns a frame now holding `page` (the
+// entry of `page` itself is published by the caller) and its old page.  The
+// shared hand advances one position per atomic (parallelPage.cu:491-509).
 template <bool DIST>
-__device__ __forceinline__ int32_t sweep(const BmView& b, uint32_t page, uint32_t slot, uint32_t batch,
-                                         uint32_t* old_page) {
+__device__ __forceinline__ int32_t sweep(const BmView& b, uint32_t page, uint32_t slot, uint32_t* old_page) {
     if constexpr (DIST) return sweep_private(b, page, slot, old_page);
-    unsigned long long res = 0;
-    uint32_t res_left = 0;
-    int32_t out = -1;
     for (uint32_t i = 0; i < b.max_sweep; ++i) {
-        if (res_left == 0u) {
-            res = atomicAdd(b.single_hand, (unsigned long long)batch);
-            res_left = batch;
-        }
-        const uint32_t f = (uint32_t)((res + (batch - res_left)) % b.n_frames);
-        --res_left;
-        unsigned long long s = __ldcg(b.frame_state + f);
-        if ((uint32_t)s != 0u) continue;                    // pinned
-        if (b.ref[f]) { b.ref[f] = 0; continue; }           // second chance
-        unsigned long long ns = ((unsigned long long)page << 32) | 1ull;
-        if (atomicCAS(b.frame_state + f, s, ns) == s) {
-            *old_page = (uint32_t)(s >> 32);
-            out = (int32_t)f;
-            break;
-        }
+        const uint32_t f = (uint32_t)(atomicAdd(b.single_hand, 1ull) % b.n_frames);
+        uint32_t q;
+        unsigned long long e = 0;
+        if (examine(b, f, &q, &e) && take_frame(b, f, q, e, page, old_page)) return (int32_t)f;
     }
-    return out;
+    return -1;
 }
 
-struct BmAcc {
-    unsigned long long hits = 0, misses = 0, evictions = 0, failures = 0, timeouts = 0;
-};
-
-// Adds k pins to frame f if it holds `page`; otherwise leaves it unchanged
-// (the add is taken back) and returns false.
-__device__ __forceinline__ bool pin_if_owner(const BmView& b, int32_t f, uint32_t page, uint32_t k) {
-    const unsigned long long old = atomicAdd(b.frame_state + f, (unsigned long long)k);
-    if ((uint32_t)(old >> 32) == page) return true;
-    atomicAdd(b.frame_state + f, 0ull - (unsigned long long)k);
-    return false;
+__device__ __forceinline__ void copy_frame(const BmView& b, uint32_t page, int32_t h) {
+    const int4* src = reinterpret_cast<const int4*>(b.backing + (size_t)page * b.frame_size);
+    int4* dst = reinterpret_cast<int4*>(b.frames + (size_t)h * b.frame_size);
+    for (uint32_t k = 0; k < b.frame_size / 16u; ++k) dst[k] = src[k];
 }
 
+// Takes k pins of `page` off its entry; the last request to leave a failed
+// load clears the failure.
+__device__ __forceinline__ void leave(const BmView& b, uint32_t page, uint32_t k) {
+    const unsigned long long old = atomicAdd(b.pt + page, 0ull - (unsigned long long)k);
+    if (e_frame(old) == kFailed && e_pins(old) == k) atomicCAS(b.pt + page, kEntryFailed, kEntryNotResident);
+}
+
+// The loader's end of a load: publish frame h (entry loading -> h, reference
+// bit set) or, when no frame was found, mark the load failed and take the
+// loader's own k pins off.
+__device__ __forceinline__ void publish(const BmView& b, uint32_t page, int32_t h, uint32_t old_page, uint32_t k,
+                                        BmAcc& acc) {
+    if (h >= 0) {
+        if (old_page != kEmptyPage) ++acc.evictions;
+        __threadfence();   // frame_page and the frame's bytes before the entry
+        atomicAdd(b.pt + page, (unsigned long long)(h - kLoading) * kFrameUnit + kRef);
+        acc.misses += 1u;
+        acc.hits += k - 1u;
+    } else {
+        const unsigned long long old = atomicAdd(b.pt + page, (0ull - kFrameUnit) - (unsigned long long)k);
+        if (e_pins(old) == k) atomicCAS(b.pt + page, kEntryFailed, kEntryNotResident);
+        acc.failures += k;
+    }
+}
+
+enum : int { kStHit = 1, kStLoad = 2, kStWait = 3 };
+
+// The first step of a fetch of `page` for k requests: add their pins.
+// Returns the state and, for a hit, the frame.
+__device__ __forceinline__ int begin_fetch(const BmView& b, uint32_t page, uint32_t k, int32_t* frame) {
+    const unsigned long long old = atomicAdd(b.pt + page, (unsigned long long)k);
+    const int32_t f = e_frame(old);
+    if (f >= 0) {
+        if (!e_ref(old)) atomicOr(b.pt + page, kRef);
+        *frame = f;
+        return kStHit;
+    }
+    if (f == kNotResident && e_pins(old) == 0u) {
+        atomicAdd(b.pt + page, 0ull - kFrameUnit);   // not resident -> loading
+        return kStLoad;
+    }
+    return kStWait;
+}
+
+// A request whose pins are registered on a page another request is loading:
+// wait (bounded) for the frame.  Returns the frame, kFailed if that load
+// failed, or kLoading if the wait ran out.
+__device__ __forceinline__ int32_t wait_loaded(const BmView& b, uint32_t page) {
+    for (uint32_t i = 0; i < kFetchSpinLimit; ++i) {
+        const int32_t f = e_frame(__ldcg(b.pt + page));
+        if (f >= 0 || f == kFailed) return f;
+        __nanosleep(32);
+    }
+    return kLoading;
+}
+
+// A whole fetch of `page` for k requests by one thread (the single-thread
+// replay, and the per-slot-hand policy).
 template <bool DIST>
-__device__ __forceinline__ int32_t fetch(const BmView& b, uint32_t page, uint32_t slot, uint32_t batch, BmAcc& acc) {
-    for (uint32_t attempt = 0; attempt < kFetchSpinLimit; ++attempt) {
-        int32_t f = __ldcg(b.page_table + page);
-        if (f >= 0) {
-            if (pin_if_owner(b, f, page, 1u)) {
-                b.ref[f] = 1;
-                ++acc.hits;
-                return f;
-            }
-            continue;   // the frame changed owner: read the page table again
+__device__ __forceinline__ int32_t fetch_k(const BmView& b, uint32_t page, uint32_t slot, uint32_t k, BmAcc& acc) {
+    for (uint32_t attempt = 0; attempt < kFetchAttempts; ++attempt) {
+        int32_t f = -1;
+        const int st = begin_fetch(b, page, k, &f);
+        if (st == kStHit) {
+            acc.hits += k;
+            return f;
         }
-        if (f == -1) {
-            if (atomicCAS(b.page_table + page, -1, kLoading) != -1) continue;
+        if (st == kStLoad) {
             uint32_t old_page = kEmptyPage;
-            int32_t h = sweep<DIST>(b, page, slot, batch, &old_page);
-            if (h < 0) {
-                atomicExch(b.page_table + page, -1);
-                ++acc.failures;
-                return -1;
-            }
-            if (old_page != kEmptyPage) {
-                atomicExch(b.page_table + old_page, -1);
-                ++acc.evictions;
-            }
-            if (b.backing && b.frames) {
-                const int4* src = reinterpret_cast<const int4*>(b.backing + (size_t)page * b.frame_size);
-                int4* dst = reinterpret_cast<int4*>(b.frames + (size_t)h * b.frame_size);
-                for (uint32_t k = 0; k < b.frame_size / 16u; ++k) dst[k] = src[k];
-            }
-            b.ref[h] = 1;
-            __threadfence();
-            atomicExch(b.page_table + page, h);
-            ++acc.misses;
+            const int32_t h = sweep<DIST>(b, page, slot, &old_page);
+            if (h >= 0 && b.backing && b.frames) copy_frame(b, page, h);
+            publish(b, page, h, old_page, k, acc);
             return h;
         }
-        __nanosleep(32);   // another request is loading this page
+        f = wait_loaded(b, page);
+        if (f >= 0) {
+            acc.hits += k;
+            return f;
+        }
+        leave(b, page, k);
+        if (f == kLoading) {
+            acc.timeouts += k;
+            return -1;
+        }
+        __nanosleep(64);   // the failed load is being left: try again
     }
-    ++acc.timeouts;
+    acc.timeouts += k;
     return -1;
 }
 
 // Warp-cooperative CLOCK sweep on the single hand.  The lanes in `loaders`
-// (each the loader of its own `page`, its page-table entry already set to
-// loading) need victim frames.  Per batch the warp takes 32 consecutive hand
-// positions with one atomicAdd and every lane examines one frame, as the
-// one-thread sweep does: a pinned frame is passed, a referenced one loses its
-// reference bit (second chance), an unpinned unreferenced one is a candidate.
-// Candidates go in hand order to the loaders in lane order, each taken with
-// the one-thread sweep's CAS (a pin that arrived in between makes it fail and
-// the loader waits for the next batch); candidates beyond the loaders' need
-// are passed.  A loader gives up after its max_sweep positions.  So a miss
-// costs about one batch of round trips instead of one per frame examined.
-// The whole warp calls converged; returns the lane's frame (-1 if none) and
-// the page it held.
+// (each the loader of its own `page`, its entry already marked loading) need
+// victim frames.  Per batch the warp takes 32 consecutive hand positions
+// with one atomicAdd and every lane examines one frame, as the one-thread
+// sweep does.  Candidates go in hand order to the loaders in lane order,
+// each taken with the one-thread sweep's compare-and-swap (a pin that
+// arrived in between makes it fail and the loader waits for the next
+// batch); candidates beyond the loaders' need are passed.  A loader gives up
+// after its max_sweep positions.  The whole warp calls converged; returns
+// the lane's frame (-1 if none) and the page it held.
 __device__ __forceinline__ int32_t sweep_warp(const BmView& b, uint32_t loaders, uint32_t page,
                                               uint32_t* old_page) {
     const uint32_t lane = threadIdx.x & 31u;
@@ -221,53 +291,37 @@ __device__ __forceinline__ int32_t sweep_warp(const BmView& b, uint32_t loaders,
         if (lane == 0u) base = atomicAdd(b.single_hand, 32ull);
         base = __shfl_sync(0xffffffffu, base, 0);
         const uint32_t f = (uint32_t)((base + lane) % b.n_frames);
-        const unsigned long long st = __ldcg(b.frame_state + f);
-        bool cand = false;
-        if ((uint32_t)st == 0u) {                   // unpinned
-            if (b.ref[f]) b.ref[f] = 0;             // second chance
-            else cand = true;
-        }
+        uint32_t q = kEmptyPage;
+        unsigned long long e = 0;
+        const bool cand = examine(b, f, &q, &e) != 0;
         const uint32_t cm = __ballot_sync(0xffffffffu, cand);
         const int n_load = __popc(loaders);
         // candidate of rank k serves the loader of rank k
         const int k = __popc(cm & lt);
         const int target = (cand && k < n_load) ? (int)nth_set_bit(loaders, k) : -1;
         const uint32_t tpage = __shfl_sync(0xffffffffu, page, target < 0 ? (int)lane : target);
-        bool took = false;
-        if (target >= 0) {
-            const unsigned long long ns = ((unsigned long long)tpage << 32) | 1ull;
-            took = atomicCAS(b.frame_state + f, st, ns) == st;
-        }
+        uint32_t victim_old = kEmptyPage;
+        const bool took = target >= 0 && take_frame(b, f, q, e, tpage, &victim_old);
         const uint32_t tm = __ballot_sync(0xffffffffu, took);
         const bool is_loader = (loaders >> lane) & 1u;
         const int r = __popc(loaders & lt);
         const int src = (is_loader && r < __popc(cm)) ? (int)nth_set_bit(cm, r) : -1;
         const uint32_t got_f = __shfl_sync(0xffffffffu, f, src < 0 ? (int)lane : src);
-        const unsigned long long got_s = __shfl_sync(0xffffffffu, st, src < 0 ? (int)lane : src);
+        const uint32_t got_old = __shfl_sync(0xffffffffu, victim_old, src < 0 ? (int)lane : src);
         if (src >= 0 && ((tm >> src) & 1u)) {
             out = (int32_t)got_f;
-            *old_page = (uint32_t)(got_s >> 32);
+            *old_page = got_old;
         }
         loaders = __ballot_sync(0xffffffffu, is_loader && out < 0);
     }
     return out;
 }
 
-// The loaders' side of a cooperative miss: unmap the victims' old pages, copy
-// each new page from the backing store with the whole warp (one loader at a
-// time, 16 bytes per lane per step), then publish the page-table entries.
-// The whole warp calls converged; h = the lane's frame from sweep_warp.
+// The loaders' side of a cooperative miss: copy each new page from the
+// backing store with the whole warp (one loader at a time, 16 bytes per lane
+// per step), then publish the entries.  The whole warp calls converged.
 __device__ __forceinline__ void finish_loads_warp(const BmView& b, bool loader, uint32_t page, int32_t h,
-                                                  uint32_t old_page, BmAcc& acc) {
-    if (loader) {
-        if (h < 0) {
-            atomicExch(b.page_table + page, -1);
-            ++acc.failures;
-        } else if (old_page != kEmptyPage) {
-            atomicExch(b.page_table + old_page, -1);
-            ++acc.evictions;
-        }
-    }
+                                                  uint32_t old_page, uint32_t k, BmAcc& acc) {
     if (b.backing && b.frames) {
         const uint32_t lane = threadIdx.x & 31u;
         const uint32_t n16 = b.frame_size / 16u;
@@ -279,29 +333,26 @@ __device__ __forceinline__ void finish_loads_warp(const BmView& b, bool loader, 
             const int32_t fr = __shfl_sync(0xffffffffu, h, l);
             const int4* src = reinterpret_cast<const int4*>(b.backing + (size_t)pg * b.frame_size);
             int4* dst = reinterpret_cast<int4*>(b.frames + (size_t)fr * b.frame_size);
-            for (uint32_t k = lane; k < n16; k += 32u) dst[k] = src[k];
+            for (uint32_t j = lane; j < n16; j += 32u) dst[j] = src[j];
         }
-        __threadfence();
         __syncwarp();
     }
-    if (loader && h >= 0) {
-        b.ref[h] = 1;
-        __threadfence();
-        atomicExch(b.page_table + page, h);
-        ++acc.misses;
-    }
+    if (loader) publish(b, page, h, old_page, k, acc);
 }
 
-// Releases k pins of frame f with one atomic.  A release of more pins than
-// the frame holds (a caller error) is taken back and counted as bad; its
-// subtraction can borrow from the page field for that instant, which makes a
-// racing fetch see another page and retry, and a racing sweep's CAS fail.
+// Releases k pins of frame f (through the page it holds) with one atomic.
+// A release of more pins than the page holds (a caller error) is taken back
+// and counted as bad.
 __device__ __forceinline__ void unpin_k(const BmView& b, int32_t f, uint32_t k, unsigned long long& ok,
                                         unsigned long long& bad) {
     if (f < 0 || (uint32_t)f >= b.n_frames || k == 0u) return;
-    const unsigned long long old = atomicAdd(b.frame_state + f, 0ull - (unsigned long long)k);
-    if ((uint32_t)old < k) {
-        atomicAdd(b.frame_state + f, (unsigned long long)k);
+    const uint32_t q = __ldcg(b.frame_page + f);
+    if (q >= b.n_logical) { bad += k; return; }
+    const unsigned long long e = __ldcg(b.pt + q);
+    if (e_frame(e) != f || e_pins(e) < k) { bad += k; return; }
+    const unsigned long long old = atomicAdd(b.pt + q, 0ull - (unsigned long long)k);
+    if (e_frame(old) != f || e_pins(old) < k) {
+        atomicAdd(b.pt + q, (unsigned long long)k);
         bad += k;
         return;
     }
@@ -339,12 +390,13 @@ __global__ void __launch_bounds__(256) k_round(BmView b, const int32_t* release_
         for (uint32_t i = 0; i < n; ++i) {
             int32_t p = pages[i];
             int32_t f = -1;
-            if (p >= 0 && (uint32_t)p < b.n_logical) f = fetch<DIST>(b, (uint32_t)p, (slot0 + i) % b.n_arms, 1u, acc);
+            if (p >= 0 && (uint32_t)p < b.n_logical) f = fetch_k<DIST>(b, (uint32_t)p, (slot0 + i) % b.n_arms, 1u, acc);
             frames_out[i] = f;
         }
     } else {
-        // warp-uniform trip count (blockDim is a multiple of 32), so the warp
-        // can merge the pins of lanes fetching the same page
+        // warp-uniform trip count (blockDim is a multiple of 32); the lanes
+        // fetching one page merge into their leader, whose atomic pins the
+        // page for all of them
         const uint32_t lane = threadIdx.x & 31u;
         for (uint64_t base = tid - lane; base < n; base += nthr) {
             const uint64_t i = base + lane;
@@ -353,38 +405,45 @@ __global__ void __launch_bounds__(256) k_round(BmView b, const int32_t* release_
             const uint32_t key = valid ? (uint32_t)p : 0x80000000u + lane;   // invalid lanes never merge
             const uint32_t peers = __match_any_sync(0xffffffffu, key);
             const uint32_t leader = (uint32_t)__ffs((int)peers) - 1u;
-            int32_t hit = -1, f0 = kLoading;
-            if (valid && lane == leader) {
-                f0 = __ldcg(b.page_table + p);
-                if (f0 >= 0 && pin_if_owner(b, f0, (uint32_t)p, (uint32_t)__popc(peers))) {
-                    b.ref[f0] = 1;
-                    hit = f0;
-                }
-            }
-            hit = __shfl_sync(0xffffffffu, hit, (int)leader);
+            const uint32_t k = (uint32_t)__popc(peers);
+            const bool lead = valid && lane == leader;
+            const uint32_t slot = (slot0 + (uint32_t)i) % b.n_arms;
             int32_t f = -1;
-            bool loader = false;
+            int st = 0;
+            if (lead) st = begin_fetch(b, (uint32_t)p, k, &f);
+            if (st == kStHit) acc.hits += k;
             if constexpr (!DIST) {
-                // single hand: the leaders of pages that are not resident become
-                // their loaders and sweep together; the other lanes fetch as below
-                // (their pages are resident, or being loaded, by then)
-                if (hit < 0 && valid && lane == leader)
-                    loader = f0 == -1 && atomicCAS(b.page_table + p, -1, kLoading) == -1;
-                const uint32_t lm = __ballot_sync(0xffffffffu, loader);
+                // the single hand's loaders sweep together
+                const uint32_t lm = __ballot_sync(0xffffffffu, st == kStLoad);
                 if (lm) {
                     uint32_t old_page = kEmptyPage;
                     const int32_t h = sweep_warp(b, lm, (uint32_t)p, &old_page);
-                    finish_loads_warp(b, loader, (uint32_t)p, h, old_page, acc);
-                    if (loader) f = h;
+                    finish_loads_warp(b, st == kStLoad, (uint32_t)p, h, old_page, k, acc);
+                    if (st == kStLoad) f = h;
+                }
+            } else if (st == kStLoad) {
+                uint32_t old_page = kEmptyPage;
+                const int32_t h = sweep_private(b, (uint32_t)p, slot, &old_page);
+                if (h >= 0 && b.backing && b.frames) copy_frame(b, (uint32_t)p, h);
+                publish(b, (uint32_t)p, h, old_page, k, acc);
+                f = h;
+            }
+            if (st == kStWait) {
+                f = wait_loaded(b, (uint32_t)p);
+                if (f >= 0) {
+                    acc.hits += k;
+                } else {
+                    leave(b, (uint32_t)p, k);
+                    if (f == kLoading) {
+                        acc.timeouts += k;
+                        f = -1;
+                    } else {
+                        f = fetch_k<DIST>(b, (uint32_t)p, slot, k, acc);   // the load failed: try once more
+                    }
                 }
             }
-            if (hit >= 0) {
-                f = hit;
-                ++acc.hits;
-            } else if (valid && !loader) {
-                f = fetch<DIST>(b, (uint32_t)p, (slot0 + (uint32_t)i) % b.n_arms, kHandBatch, acc);
-            }
-            if (i < n) frames_out[i] = f;
+            f = __shfl_sync(0xffffffffu, f, (int)leader);
+            if (i < n) frames_out[i] = valid ? f : -1;
         }
     }
     block_add_counters<7>({ok, bad, acc.hits, acc.misses, acc.evictions, acc.failures, acc.timeouts},
@@ -395,17 +454,15 @@ __global__ void __launch_bounds__(256) k_round(BmView b, const int32_t* release_
 __global__ void k_bm_init(BmView b) {
     const uint64_t tid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
     const uint64_t nthr = (uint64_t)gridDim.x * blockDim.x;
-    for (uint64_t p = tid; p < b.n_logical; p += nthr) b.page_table[p] = -1;
-    for (uint64_t f = tid; f < b.n_frames; f += nthr) {
-        b.frame_state[f] = (unsigned long long)kEmptyPage << 32;
-        b.ref[f] = 0;
-    }
+    for (uint64_t p = tid; p < b.n_logical; p += nthr) b.pt[p] = kEntryNotResident;
+    for (uint64_t f = tid; f < b.n_frames; f += nthr) b.frame_page[f] = kEmptyPage;
     for (uint64_t a = tid; a < b.n_arms; a += nthr)
         b.arms[a] = (uint32_t)(((unsigned long long)a * b.n_frames) / b.n_arms);
     if (tid == 0) *b.single_hand = 0ull;
 }
 
-// Consistency check: page_table and frame_state are inverse maps; pins sum.
+// Consistency check: the entries and frame_page are inverse maps, nothing is
+// left loading, pins sum.
 struct BmCheck {
     unsigned long long resident, mapped_frames, mismatches, loading, pins;
 };
@@ -415,19 +472,22 @@ __global__ void k_bm_check(BmView b, BmCheck* out) {
     const uint64_t nthr = (uint64_t)gridDim.x * blockDim.x;
     unsigned long long res = 0, mapped = 0, mism = 0, loading = 0, pins = 0;
     for (uint64_t p = tid; p < b.n_logical; p += nthr) {
-        int32_t f = b.page_table[p];
-        if (f == kLoading) { ++loading; continue; }
-        if (f < 0) continue;
+        const unsigned long long e = b.pt[p];
+        const int32_t f = e_frame(e);
+        pins += e_pins(e);
+        if (f == kLoading || f == kFailed) { ++loading; continue; }
+        if (f < 0) {
+            if (e_pins(e) || e_ref(e)) ++mism;   // pins or a reference bit on a page no frame holds
+            continue;
+        }
         ++res;
-        if ((uint32_t)f >= b.n_frames || (uint32_t)(b.frame_state[f] >> 32) != p) ++mism;
+        if ((uint32_t)f >= b.n_frames || b.frame_page[f] != p) ++mism;
     }
     for (uint64_t f = tid; f < b.n_frames; f += nthr) {
-        unsigned long long s = b.frame_state[f];
-        uint32_t pg = (uint32_t)(s >> 32);
-        pins += (uint32_t)s;
+        const uint32_t pg = b.frame_page[f];
         if (pg == kEmptyPage) continue;
         ++mapped;
-        if (pg >= b.n_logical || b.page_table[pg] != (int32_t)f) ++mism;
+        if (pg >= b.n_logical || e_frame(b.pt[pg]) != (int32_t)f) ++mism;
     }
     if (res) atomicAdd(&out->resident, res);
     if (mapped) atomicAdd(&out->mapped_frames, mapped);
@@ -457,6 +517,7 @@ struct pbm_bufmgr {
     BmView v;
     BmCheck* d_check;
     size_t frames_bytes;
+    int device;   // the device current at create: every later call runs there
 };
 
 extern "C" {
@@ -469,6 +530,7 @@ int pbm_bufmgr_create(const pbm_bufmgr_config* cfg, const void* d_backing, pbm_b
     pbm_bufmgr* m = new (std::nothrow) pbm_bufmgr();
     if (!m) return PBM_ERR_NOMEM;
     std::memset((void*)m, 0, sizeof(*m));
+    cudaGetDevice(&m->device);
     BmView& b = m->v;
     b.n_logical = (uint32_t)cfg->n_logical;
     b.n_frames = cfg->n_frames;
@@ -477,9 +539,8 @@ int pbm_bufmgr_create(const pbm_bufmgr_config* cfg, const void* d_backing, pbm_b
     b.n_arms = cfg->n_arms ? cfg->n_arms : 1u;
     b.dist = cfg->policy;
     b.backing = (const char*)d_backing;
-    bool ok = cudaMalloc(&b.page_table, sizeof(int32_t) * b.n_logical) == cudaSuccess &&
-              cudaMalloc(&b.frame_state, sizeof(unsigned long long) * b.n_frames) == cudaSuccess &&
-              cudaMalloc(&b.ref, b.n_frames) == cudaSuccess &&
+    bool ok = cudaMalloc(&b.pt, sizeof(unsigned long long) * b.n_logical) == cudaSuccess &&
+              cudaMalloc(&b.frame_page, sizeof(uint32_t) * b.n_frames) == cudaSuccess &&
               cudaMalloc(&b.single_hand, sizeof(unsigned long long)) == cudaSuccess &&
               cudaMalloc(&b.arms, sizeof(uint32_t) * b.n_arms) == cudaSuccess &&
               cudaMalloc(&b.stats, sizeof(BmStats)) == cudaSuccess &&
@@ -502,10 +563,10 @@ int pbm_bufmgr_create(const pbm_bufmgr_config* cfg, const void* d_backing, pbm_b
 
 int pbm_bufmgr_destroy(pbm_bufmgr* m) {
     if (!m) return PBM_ERR_INVALID;
+    pbm::DeviceScope scope(m->device);
     cudaDeviceSynchronize();
-    cudaFree(m->v.page_table);
-    cudaFree(m->v.frame_state);
-    cudaFree(m->v.ref);
+    cudaFree(m->v.pt);
+    cudaFree(m->v.frame_page);
     cudaFree(m->v.single_hand);
     cudaFree(m->v.arms);
     cudaFree(m->v.stats);
@@ -517,6 +578,7 @@ int pbm_bufmgr_destroy(pbm_bufmgr* m) {
 
 int pbm_bufmgr_reset(pbm_bufmgr* m, void* stream) {
     if (!m) return PBM_ERR_INVALID;
+    pbm::DeviceScope scope(m->device);
     cudaStream_t s = (cudaStream_t)stream;
     k_bm_init<<<sm_count() * 4, 256, 0, s>>>(m->v);
     PBM_LAUNCH_CHECK();
@@ -529,6 +591,7 @@ int pbm_bufmgr_round(pbm_bufmgr* m, const int32_t* d_frames_of, const int32_t* d
                      int32_t* d_frames_out, int serial, void* stream) {
     if (!m || (n_release && (!d_frames_of || !d_release_idx)) || (n && (!d_pages || !d_frames_out)))
         return PBM_ERR_INVALID;
+    pbm::DeviceScope scope(m->device);
     if (n == 0 && n_release == 0) return PBM_OK;
     const uint32_t work = n > n_release ? n : n_release;
     int block = serial ? 1 : 256;
@@ -545,6 +608,7 @@ int pbm_bufmgr_round(pbm_bufmgr* m, const int32_t* d_frames_of, const int32_t* d
 
 int pbm_bufmgr_stats(pbm_bufmgr* m, pbm_bufmgr_counters* h_out, void* stream) {
     if (!m || !h_out) return PBM_ERR_INVALID;
+    pbm::DeviceScope scope(m->device);
     cudaStream_t s = (cudaStream_t)stream;
     BmStats d;
     PBM_CUDA_TRY(cudaMemcpyAsync(&d, m->v.stats, sizeof(d), cudaMemcpyDeviceToHost, s));
@@ -561,6 +625,7 @@ int pbm_bufmgr_stats(pbm_bufmgr* m, pbm_bufmgr_counters* h_out, void* stream) {
 
 int pbm_bufmgr_check(pbm_bufmgr* m, pbm_bufmgr_check_result* h_out, void* stream) {
     if (!m || !h_out) return PBM_ERR_INVALID;
+    pbm::DeviceScope scope(m->device);
     cudaStream_t s = (cudaStream_t)stream;
     PBM_CUDA_TRY(cudaMemsetAsync(m->d_check, 0, sizeof(BmCheck), s));
     k_bm_check<<<sm_count() * 4, 256, 0, s>>>(m->v, m->d_check);
@@ -581,10 +646,25 @@ int pbm_bufmgr_gather(pbm_bufmgr* m, const int32_t* d_frame_ids, uint32_t n, uin
     if (!m || !m->v.frames || (n && (!d_frame_ids || !d_out)) || bytes_per_frame == 0 ||
         bytes_per_frame > m->v.frame_size || (bytes_per_frame & 3u))
         return PBM_ERR_INVALID;
+    pbm::DeviceScope scope(m->device);
     if (n == 0) return PBM_OK;
     k_bm_gather<<<sm_count() * 4, 256, 0, (cudaStream_t)stream>>>(m->v, d_frame_ids, n, bytes_per_frame / 4u,
                                                                   d_out);
     PBM_LAUNCH_CHECK();
+    return PBM_OK;
+}
+
+int pbm_bufmgr_read_tables(pbm_bufmgr* m, uint64_t* h_page_entries, uint32_t* h_frame_pages, void* stream) {
+    if (!m || (!h_page_entries && !h_frame_pages)) return PBM_ERR_INVALID;
+    pbm::DeviceScope scope(m->device);
+    cudaStream_t s = (cudaStream_t)stream;
+    if (h_page_entries)
+        PBM_CUDA_TRY(cudaMemcpyAsync(h_page_entries, m->v.pt, sizeof(uint64_t) * m->v.n_logical,
+                                     cudaMemcpyDeviceToHost, s));
+    if (h_frame_pages)
+        PBM_CUDA_TRY(cudaMemcpyAsync(h_frame_pages, m->v.frame_page, sizeof(uint32_t) * m->v.n_frames,
+                                     cudaMemcpyDeviceToHost, s));
+    PBM_CUDA_TRY(cudaStreamSynchronize(s));
     return PBM_OK;
 }
 

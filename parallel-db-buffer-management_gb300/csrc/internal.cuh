@@ -50,6 +50,25 @@ __device__ __forceinline__ void block_add_counters(const unsigned long long (&v)
     __syncthreads();
     if (threadIdx.x < (unsigned)N && sh[threadIdx.x]) atomicAdd(dst[threadIdx.x], sh[threadIdx.x]);
 }
+// Makes a device current for the rest of the calling scope and restores the
+// caller's device when the scope ends.  Every entry point that takes a pool
+// (or an object built on one) opens one with the pool's device, so a process
+// may hold one pool per GPU and call into any of them from any current
+// device.  A negative ordinal (no pool) switches nothing.
+struct DeviceScope {
+    int prev = -1;
+    bool switched = false;
+    explicit DeviceScope(int dev) {
+        if (dev >= 0 && cudaGetDevice(&prev) == cudaSuccess && prev != dev && cudaSetDevice(dev) == cudaSuccess)
+            switched = true;
+    }
+    ~DeviceScope() {
+        if (switched) cudaSetDevice(prev);
+    }
+    DeviceScope(const DeviceScope&) = delete;
+    DeviceScope& operator=(const DeviceScope&) = delete;
+};
+
 constexpr int kDefaultBlock = 256;
 constexpr int kCappedBlocks = 5;   // resident blocks the register-capped batch kernels are built for
 
@@ -76,6 +95,11 @@ struct pbm_pool {
     pbm::CheckCounters* d_check;
     unsigned long long* d_scan;     // scratch for prefix sums (per-block partials)
     unsigned long long* d_prefix;   // batch prefix (n_groups + 1)
+    pbm::LaunchBudget* d_budget;    // fail-fast launch budget: free pages at launch start
+    int32_t* d_free_list;           // the budget pass's list of free pages (list mode)
+    uint64_t free_list_cap;
+    unsigned long long* d_budget_blocks;   // free pages per block slice of the budget pass
+    uint32_t budget_blocks;
     uint32_t prefix_cap;
     int device;
 };
@@ -90,6 +114,8 @@ struct pbm_pool {
             return PBM_ERR_CUDA;                                                    \
         }                                                                           \
     } while (0)
+
+#define PBM_ON_POOL_DEVICE(pool) pbm::DeviceScope pbm_device_scope_((pool) ? (pool)->device : -1)
 
 #define PBM_LAUNCH_CHECK()                                                          \
     do {                                                                            \
@@ -106,4 +132,8 @@ namespace pbm {
 // Implemented in pool.cu
 int fifo_build(pbm_pool* pool, cudaStream_t s);
 int popcount_used(pbm_pool* pool, uint64_t* used, cudaStream_t s);
+// Counts the pool's free pages into pool->d_budget on stream s (no sync); a
+// launch of n_requests that asks for at least half of them also gets them
+// listed in order in pool->d_free_list (list mode, when they fit).
+int budget_prepare(pbm_pool* pool, uint64_t n_requests, cudaStream_t s);
 }  // namespace pbm

@@ -343,6 +343,7 @@ int graph_impl(pbm_pool* pool, bool queue, const pbm_group* d_groups, uint32_t n
     cudaStream_t s = (cudaStream_t)stream;
     pbm_graph* g = new (std::nothrow) pbm_graph();
     if (!g) return PBM_ERR_NOMEM;
+    g->device = pool->device;
     g->graph = nullptr;
     g->exec = nullptr;
     if (cudaMalloc(&g->d_step, sizeof(uint32_t)) != cudaSuccess ||
@@ -404,6 +405,7 @@ int graph_impl(pbm_pool* pool, bool queue, const pbm_group* d_groups, uint32_t n
 extern "C" {
 
 int pbm_malloc_init(pbm_pool* pool) {
+    PBM_ON_POOL_DEVICE(pool);
     std::lock_guard<std::mutex> lk(g_reg_mu);
     int rc = check_pool(pool);
     if (rc) return rc;
@@ -429,6 +431,7 @@ int pbm_malloc_init(pbm_pool* pool) {
 }
 
 int pbm_malloc_tables(pbm_pool* pool, void** d_start_of, void** d_live, void** d_len_of) {
+    PBM_ON_POOL_DEVICE(pool);
     std::lock_guard<std::mutex> lk(g_reg_mu);
     MallocTables* t = tables_of(pool);
     if (!t || !t->start_of) return PBM_ERR_INVALID;
@@ -439,6 +442,7 @@ int pbm_malloc_tables(pbm_pool* pool, void** d_start_of, void** d_live, void** d
 }
 
 int pbm_malloc_release(pbm_pool* pool) {
+    PBM_ON_POOL_DEVICE(pool);
     std::lock_guard<std::mutex> lk(g_reg_mu);
     MallocTables* t = tables_of(pool);
     if (!t) return PBM_ERR_INVALID;
@@ -457,6 +461,7 @@ int pbm_malloc_release(pbm_pool* pool) {
 int pbm_malloc_batch(pbm_pool* pool, const pbm_group* d_groups, const pbm_group* h_groups, uint32_t n_groups,
                      const uint32_t* d_sizes, unsigned long long* d_ptrs, uint64_t arena_len, uint32_t seed,
                      uint32_t max_steps, int mode, void* stream) {
+    PBM_ON_POOL_DEVICE(pool);
     std::lock_guard<std::mutex> lk(g_reg_mu);
     return batch_impl(pool, false, d_groups, h_groups, n_groups, d_sizes, d_ptrs, arena_len, seed, max_steps, mode,
                       stream);
@@ -465,12 +470,14 @@ int pbm_malloc_batch(pbm_pool* pool, const pbm_group* d_groups, const pbm_group*
 int pbm_malloc_graph_create(pbm_pool* pool, const pbm_group* d_groups, uint32_t n_groups, uint32_t n_steps,
                             const uint32_t* d_sizes, unsigned long long* d_ptrs, uint64_t arena_len,
                             uint32_t seed0, uint32_t max_steps, void* stream, pbm_graph** out) {
+    PBM_ON_POOL_DEVICE(pool);
     std::lock_guard<std::mutex> lk(g_reg_mu);
     return graph_impl(pool, false, d_groups, n_groups, n_steps, d_sizes, d_ptrs, arena_len, seed0, max_steps, stream,
                       out);
 }
 
 int pbm_malloc_counts(pbm_pool* pool, uint64_t* h_live_runs, uint64_t* h_bad_frees, void* stream) {
+    PBM_ON_POOL_DEVICE(pool);
     std::lock_guard<std::mutex> lk(g_reg_mu);
     MallocTables* t = tables_of(pool);
     if (!t || !t->start_of) return PBM_ERR_INVALID;
@@ -497,6 +504,7 @@ int pbm_malloc_counts(pbm_pool* pool, uint64_t* h_live_runs, uint64_t* h_bad_fre
 // ---- queue backend ----
 
 int pbm_qmalloc_init(pbm_pool* pool, uint32_t ring_capacity) {
+    PBM_ON_POOL_DEVICE(pool);
     std::lock_guard<std::mutex> lk(g_reg_mu);
     int rc = check_pool(pool);
     if (rc) return rc;
@@ -527,6 +535,7 @@ int pbm_qmalloc_init(pbm_pool* pool, uint32_t ring_capacity) {
 }
 
 int pbm_qmalloc_release(pbm_pool* pool) {
+    PBM_ON_POOL_DEVICE(pool);
     std::lock_guard<std::mutex> lk(g_reg_mu);
     MallocTables* t = tables_of(pool);
     if (!t || !t->rings) return PBM_ERR_INVALID;
@@ -539,6 +548,7 @@ int pbm_qmalloc_release(pbm_pool* pool) {
 int pbm_qmalloc_batch(pbm_pool* pool, const pbm_group* d_groups, const pbm_group* h_groups, uint32_t n_groups,
                       const uint32_t* d_sizes, unsigned long long* d_ptrs, uint64_t arena_len, uint32_t seed,
                       uint32_t max_steps, int mode, void* stream) {
+    PBM_ON_POOL_DEVICE(pool);
     std::lock_guard<std::mutex> lk(g_reg_mu);
     return batch_impl(pool, true, d_groups, h_groups, n_groups, d_sizes, d_ptrs, arena_len, seed, max_steps, mode,
                       stream);
@@ -547,6 +557,7 @@ int pbm_qmalloc_batch(pbm_pool* pool, const pbm_group* d_groups, const pbm_group
 int pbm_qmalloc_graph_create(pbm_pool* pool, const pbm_group* d_groups, uint32_t n_groups, uint32_t n_steps,
                              const uint32_t* d_sizes, unsigned long long* d_ptrs, uint64_t arena_len,
                              uint32_t seed0, uint32_t max_steps, void* stream, pbm_graph** out) {
+    PBM_ON_POOL_DEVICE(pool);
     std::lock_guard<std::mutex> lk(g_reg_mu);
     return graph_impl(pool, true, d_groups, n_groups, n_steps, d_sizes, d_ptrs, arena_len, seed0, max_steps, stream,
                       out);
@@ -554,6 +565,7 @@ int pbm_qmalloc_graph_create(pbm_pool* pool, const pbm_group* d_groups, uint32_t
 
 int pbm_qmalloc_counts(pbm_pool* pool, uint64_t* h_queued, uint64_t* h_chunks, uint64_t* h_overflow,
                        uint64_t* h_timeouts, uint64_t* h_bad_frees, void* stream) {
+    PBM_ON_POOL_DEVICE(pool);
     std::lock_guard<std::mutex> lk(g_reg_mu);
     MallocTables* t = tables_of(pool);
     if (!t || !t->rings) return PBM_ERR_INVALID;

@@ -97,6 +97,7 @@ static void monitor_loop(pbm_monitor* m) {
 extern "C" {
 
 int pbm_monitor_start(pbm_pool* pool, uint32_t interval_us, uint32_t max_samples, pbm_monitor** out) {
+    PBM_ON_POOL_DEVICE(pool);
     if (!pool || !out || max_samples == 0) return PBM_ERR_INVALID;
     *out = nullptr;
     pbm_monitor* m = new (std::nothrow) pbm_monitor();

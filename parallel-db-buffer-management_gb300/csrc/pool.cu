@@ -11,21 +11,27 @@
 
 #include <atomic>
 
+#include <algorithm>
+
 #include "internal.cuh"
 
 namespace pbm {
 
 std::atomic<unsigned long long> g_launches{0};
 
+// SM count of the current device, cached per device ordinal (one atomic
+// word each, so host threads launching at once never see a torn value).
 int sm_count() {
-    static std::atomic<int> cached{0};
-    int c = cached.load(std::memory_order_relaxed);
+    static std::atomic<int> cached[64];
+    int dev = 0;
+    cudaGetDevice(&dev);
+    std::atomic<int>* slot = (dev >= 0 && dev < 64) ? &cached[dev] : nullptr;
+    int c = slot ? slot->load(std::memory_order_relaxed) : 0;
     if (!c) {
-        int dev = 0, n = 0;
-        cudaGetDevice(&dev);
+        int n = 0;
         cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
         c = n > 0 ? n : 1;
-        cached.store(c, std::memory_order_relaxed);
+        if (slot) slot->store(c, std::memory_order_relaxed);
     }
     return c;
 }
@@ -239,6 +245,89 @@ int fifo_build(pbm_pool* pool, cudaStream_t s) {
     return PBM_OK;
 }
 
+// ---- fail-fast launch budget ----
+// Pass 1: the free pages (clear bits; padding bits stay set) of each block's
+// contiguous slice of `per` 64-bit words, into counts[block] and the totals.
+__global__ void k_free_budget(const unsigned long long* words, uint32_t n_words64, uint32_t per,
+                              unsigned long long* counts, LaunchBudget* b) {
+    const uint64_t w0 = (uint64_t)blockIdx.x * per;
+    const uint64_t w1 = min((uint64_t)n_words64, w0 + per);
+    unsigned long long c = 0;
+    for (uint64_t w = w0 + threadIdx.x; w < w1; w += blockDim.x)
+        c += (unsigned long long)__popcll(~__ldcg(words + w));
+    c = block_sum(c);
+    if (threadIdx.x == 0) {
+        counts[blockIdx.x] = c;
+        if (c) atomicAdd(reinterpret_cast<unsigned long long*>(&b->free_at_start), c);
+    }
+}
+
+// Pass 2: when the launch asks for at least half of the F free pages and the
+// list holds them, every block writes its slice's free pages in ascending
+// order at its offset (the counts of the blocks before it); list_mode says
+// whether the list is valid for this launch.
+__global__ void k_free_list(const unsigned long long* words, uint32_t n_words64, uint32_t per,
+                            const unsigned long long* counts, LaunchBudget* b, unsigned long long n_requests,
+                            int32_t* list, unsigned long long cap) {
+    __shared__ unsigned long long warp_tot[32];
+    __shared__ unsigned long long s_base;
+    const long long F = b->free_at_start;
+    const bool mode = F > 0 && 2ull * n_requests >= (unsigned long long)F && (unsigned long long)F <= cap;
+    if (blockIdx.x == 0 && threadIdx.x == 0) b->list_mode = mode ? 1 : 0;
+    if (!mode) return;
+    unsigned long long off = 0;
+    for (uint32_t k = threadIdx.x; k < blockIdx.x; k += blockDim.x) off += counts[k];
+    off = block_sum(off);
+    if (threadIdx.x == 0) s_base = off;
+    __syncthreads();
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+    const uint64_t w0 = (uint64_t)blockIdx.x * per;
+    const uint64_t w1 = min((uint64_t)n_words64, w0 + per);
+    for (uint64_t base = w0; base < w1; base += blockDim.x) {
+        const uint64_t w = base + threadIdx.x;
+        unsigned long long fr = w < w1 ? ~__ldcg(words + w) : 0ull;
+        const int c = __popcll(fr);
+        int incl = c;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            const int y = __shfl_up_sync(0xffffffffu, incl, d);
+            if (lane >= d) incl += y;
+        }
+        if (lane == 31) warp_tot[warp] = (unsigned long long)incl;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            unsigned long long acc = 0;
+            for (int i = 0; i < nwarps; ++i) { const unsigned long long t = warp_tot[i]; warp_tot[i] = acc; acc += t; }
+            warp_tot[31] = acc;   // (nwarps <= 8 here, so slot 31 is free) the chunk's total
+        }
+        __syncthreads();
+        unsigned long long pos = s_base + warp_tot[warp] + (unsigned long long)(incl - c);
+        while (fr) {
+            const int bit = __ffsll((long long)fr) - 1;
+            fr &= fr - 1ull;
+            list[pos++] = (int32_t)(w * 64u + (uint64_t)bit);
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) s_base += warp_tot[31];
+        __syncthreads();
+    }
+}
+
+int budget_prepare(pbm_pool* pool, uint64_t n_requests, cudaStream_t s) {
+    PBM_CUDA_TRY(cudaMemsetAsync(pool->d_budget, 0, sizeof(LaunchBudget), s));
+    const uint32_t nw64 = (uint32_t)(pool->bitmap_bytes / 8u);
+    const uint32_t nb = pool->budget_blocks;
+    const uint32_t per = (nw64 + nb - 1u) / nb;
+    k_free_budget<<<nb, 256, 0, s>>>(reinterpret_cast<const unsigned long long*>(pool->d_words), nw64, per,
+                                     pool->d_budget_blocks, pool->d_budget);
+    PBM_LAUNCH_CHECK();
+    k_free_list<<<nb, 256, 0, s>>>(reinterpret_cast<const unsigned long long*>(pool->d_words), nw64, per,
+                                   pool->d_budget_blocks, pool->d_budget, (unsigned long long)n_requests,
+                                   pool->d_free_list, (unsigned long long)pool->free_list_cap);
+    PBM_LAUNCH_CHECK();
+    return PBM_OK;
+}
+
 int popcount_used(pbm_pool* pool, uint64_t* used, cudaStream_t s) {
     PBM_CUDA_TRY(cudaMemsetAsync(&pool->d_check->used, 0, sizeof(unsigned long long), s));
     uint32_t nw64 = (uint32_t)(pool->bitmap_bytes / 8u);
@@ -269,6 +358,9 @@ static void pool_free_all(pbm_pool* p) {
     cudaFree(p->d_fifo);
     cudaFree(p->d_seen);
     cudaFree(p->d_check);
+    cudaFree(p->d_budget);
+    cudaFree(p->d_free_list);
+    cudaFree(p->d_budget_blocks);
     cudaFree(p->d_scan);
     cudaFree(p->d_prefix);
     delete p;
@@ -325,6 +417,10 @@ int pbm_pool_create(const pbm_pool_config* cfg, pbm_pool** out) {
     p->view.page_size = cfg->page_size;
     const uint32_t nb_scan = (uint32_t)((p->view.n_words32 + 4095u) / 4096u) + 1u;
     p->prefix_cap = 0;
+    // the budget pass: one block per 256 64-bit words, at most 4 per SM; its
+    // free list covers launches into a pool at least 75% full
+    p->budget_blocks = (uint32_t)std::min<uint64_t>((uint64_t)sm_count() * 4u, std::max<uint64_t>(1u, (nw64 + 255u) / 256u));
+    p->free_list_cap = std::max<uint64_t>(1024u, cfg->n_pages / 4u);
     bool ok = cudaMalloc(&p->d_words, p->bitmap_bytes) == cudaSuccess &&
               cudaMalloc(&p->d_stats, sizeof(DevStats)) == cudaSuccess &&
               cudaMalloc(&p->d_cursors, sizeof(int32_t) * p->max_slots) == cudaSuccess &&
@@ -333,6 +429,9 @@ int pbm_pool_create(const pbm_pool_config* cfg, pbm_pool** out) {
               cudaMalloc(&p->d_fifo, sizeof(FifoState)) == cudaSuccess &&
               cudaMalloc(&p->d_seen, p->bitmap_bytes) == cudaSuccess &&
               cudaMalloc(&p->d_check, sizeof(CheckCounters)) == cudaSuccess &&
+              cudaMalloc(&p->d_budget, sizeof(LaunchBudget)) == cudaSuccess &&
+              cudaMalloc(&p->d_free_list, sizeof(int32_t) * p->free_list_cap) == cudaSuccess &&
+              cudaMalloc(&p->d_budget_blocks, sizeof(unsigned long long) * p->budget_blocks) == cudaSuccess &&
               cudaMalloc(&p->d_scan, sizeof(unsigned long long) * nb_scan) == cudaSuccess;
     if (ok && (cfg->flags & PBM_POOL_MATERIALIZE)) {
         ok = cudaMalloc(&p->d_base, (size_t)cfg->n_pages * cfg->page_size) == cudaSuccess;
@@ -352,6 +451,7 @@ int pbm_pool_create(const pbm_pool_config* cfg, pbm_pool** out) {
 }
 
 int pbm_pool_destroy(pbm_pool* pool) {
+    PBM_ON_POOL_DEVICE(pool);
     if (!pool) return PBM_ERR_INVALID;
     cudaDeviceSynchronize();
     pbm_malloc_release(pool);   // malloc side tables, if any
@@ -371,11 +471,13 @@ int pbm_pool_info(const pbm_pool* pool, uint64_t* n_pages, uint32_t* page_size, 
 }
 
 int pbm_pool_reset(pbm_pool* pool, void* stream) {
+    PBM_ON_POOL_DEVICE(pool);
     if (!pool) return PBM_ERR_INVALID;
     return pool_reset_impl(pool, (cudaStream_t)stream);
 }
 
 int pbm_pool_prefill_bernoulli(pbm_pool* pool, double occupancy, uint64_t seed, void* stream) {
+    PBM_ON_POOL_DEVICE(pool);
     if (!pool || !(occupancy >= 0.0) || occupancy > 1.0) return PBM_ERR_INVALID;
     cudaStream_t s = (cudaStream_t)stream;
     uint64_t thresh = occupancy <= 0.0 ? 0ull
@@ -389,11 +491,13 @@ int pbm_pool_prefill_bernoulli(pbm_pool* pool, double occupancy, uint64_t seed, 
 }
 
 int pbm_pool_used(pbm_pool* pool, uint64_t* h_used, void* stream) {
+    PBM_ON_POOL_DEVICE(pool);
     if (!pool || !h_used) return PBM_ERR_INVALID;
     return popcount_used(pool, h_used, (cudaStream_t)stream);
 }
 
 int pbm_pool_read_bitmap(pbm_pool* pool, void* h_dst, size_t bytes, void* stream) {
+    PBM_ON_POOL_DEVICE(pool);
     if (!pool || !h_dst || bytes != pool->bitmap_bytes) return PBM_ERR_INVALID;
     cudaStream_t s = (cudaStream_t)stream;
     PBM_CUDA_TRY(cudaMemcpyAsync(h_dst, pool->d_words, bytes, cudaMemcpyDeviceToHost, s));
@@ -402,6 +506,7 @@ int pbm_pool_read_bitmap(pbm_pool* pool, void* h_dst, size_t bytes, void* stream
 }
 
 int pbm_pool_write_bitmap(pbm_pool* pool, const void* h_src, size_t bytes, void* stream) {
+    PBM_ON_POOL_DEVICE(pool);
     if (!pool || !h_src || bytes != pool->bitmap_bytes) return PBM_ERR_INVALID;
     cudaStream_t s = (cudaStream_t)stream;
     PBM_CUDA_TRY(cudaMemcpyAsync(pool->d_words, h_src, bytes, cudaMemcpyHostToDevice, s));
@@ -413,6 +518,7 @@ int pbm_pool_write_bitmap(pbm_pool* pool, const void* h_src, size_t bytes, void*
 }
 
 int pbm_pool_device_state(pbm_pool* pool, int build_fifo, pbm_device_state* h_out, void* stream) {
+    PBM_ON_POOL_DEVICE(pool);
     if (!pool || !h_out) return PBM_ERR_INVALID;
     if (build_fifo && !pool->fifo_valid) {
         int rc = fifo_build(pool, (cudaStream_t)stream);
@@ -436,6 +542,7 @@ int pbm_pool_device_state(pbm_pool* pool, int build_fifo, pbm_device_state* h_ou
 }
 
 int pbm_pool_stats(pbm_pool* pool, pbm_stats* h_out, void* stream) {
+    PBM_ON_POOL_DEVICE(pool);
     if (!pool || !h_out) return PBM_ERR_INVALID;
     cudaStream_t s = (cudaStream_t)stream;
     DevStats d;
@@ -450,6 +557,7 @@ int pbm_pool_stats(pbm_pool* pool, pbm_stats* h_out, void* stream) {
 
 int pbm_check_ids(pbm_pool* pool, const int32_t* d_ids, uint32_t n, pbm_check_result* h_out,
                   void* stream) {
+    PBM_ON_POOL_DEVICE(pool);
     if (!pool || !h_out || (n && !d_ids)) return PBM_ERR_INVALID;
     cudaStream_t s = (cudaStream_t)stream;
     PBM_CUDA_TRY(cudaMemsetAsync(pool->d_seen, 0, pool->bitmap_bytes, s));

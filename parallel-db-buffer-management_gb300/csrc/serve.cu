@@ -5,19 +5,31 @@
 // replay in real time from their arrival stamps.  Each tenant owns a ring of
 // page slots in device memory: ALLOC n appends n new pages, FREE n releases
 // min(n, pages the tenant holds) of its oldest pages, FETCH n pins and then
-// releases n pages of a shared fetch trace in the buffer manager.  A tenant's
-// requests are admitted in arrival order.  Admission is by free-page budget:
-// the pages free below max_occupancy when the server is created are split
-// into per-tenant quotas, and an ALLOC that would take its tenant over quota
-// is rejected at once (the tenant's own later FREEs, which could make room,
-// queue behind it, so waiting could only deadlock).  A FREE waits until the
-// pages it releases have been allocated on the device.  Admitted requests
-// of all tenants form the next batch as soon as one of n_streams batch slots
-// is free, so batches overlap on the device and requests that arrive while
-// others run join the following batch.  Bitmap, clock hands, rings and RNG
-// streams stay resident between batches.  Page counts per request depend only
-// on the tenant's own requests and quota, so a tenant gets the same results
-// alone and in a mix; only latencies change.
+// releases n pages of a shared fetch trace in the buffer manager.
+//
+// Admission is by free-page budget, shared by the whole pool: the pages free
+// below max_occupancy when the server is created.  An ALLOC is admitted when
+// the pages the tenants hold on the device (counting allocations in flight,
+// and frees only once their batch has finished) plus its own fit the budget;
+// otherwise it waits at the front of its tenant's queue until frees land.
+// Only an ALLOC that could never fit (more pages than the budget, the
+// tenant's ring or its optional quota) is rejected.  A tenant's ALLOCs keep
+// their arrival order; a later FREE may pass a waiting ALLOC when every page
+// it releases is older than that ALLOC (so it releases exactly the pages it
+// would in arrival order), and a FETCH may always pass.  A FREE waits until
+// the pages it releases have been allocated on the device.  Admitted
+// requests of all tenants form the next batch as soon as one of n_streams
+// batch slots is free, so batches overlap on the device and requests that
+// arrive while others run join the following batch.  Bitmap, clock hands,
+// rings and RNG streams stay resident between batches.
+//
+// Results: a request's status and page count depend only on its tenant's
+// own requests, so they are the same alone and in a mix for every request
+// the mix admits.  Contention changes when a request is admitted (its
+// latency), not what it gets.  The one exception: when no arrivals are left,
+// nothing is in flight and nothing can be admitted, the loop stops and the
+// requests still waiting end with status -1 (they waited for memory that no
+// remaining request frees); a tenant alone would have had that memory.
 #include <algorithm>
 #include <chrono>
 #include <deque>
@@ -47,6 +59,7 @@ struct BatchSlot {
     cudaStream_t stream = nullptr;
     cudaEvent_t done = nullptr;
     bool busy = false;
+    uint64_t freed_pages = 0;        // pages the batch releases (back in the budget when it finishes)
     pbm_group* h_groups = nullptr;   // pinned
     pbm_group* d_groups = nullptr;
     int32_t* d_frames = nullptr;
@@ -68,7 +81,9 @@ struct pbm_server {
     uint32_t max_groups;
     uint32_t max_fetch;
     uint64_t n_pages;
-    uint64_t quota;                  // pages a tenant may hold
+    uint64_t budget;                 // pages the tenants may hold together
+    uint64_t quota;                  // pages one tenant may hold (UINT64_MAX: no per-tenant cap)
+    uint64_t device_held;            // pages held or being allocated on the device by the tenants
     uint32_t seed;
     uint64_t fetch_cursor;
     std::vector<Tenant> tenants;
@@ -78,6 +93,7 @@ extern "C" {
 
 int pbm_server_create(pbm_pool* pool, pbm_bufmgr* bm, const int32_t* d_fetch_pages, uint64_t n_fetch_pages,
                       const pbm_server_config* cfg, pbm_server** out) {
+    PBM_ON_POOL_DEVICE(pool);
     if (!pool || !cfg || !out || cfg->n_tenants == 0 || cfg->ring_pages == 0 || cfg->n_streams == 0 ||
         cfg->max_batch_requests == 0 || cfg->max_batch_requests > 2048 || !(cfg->max_occupancy > 0.0) ||
         cfg->max_occupancy > 1.0)
@@ -97,15 +113,14 @@ int pbm_server_create(pbm_pool* pool, pbm_bufmgr* bm, const int32_t* d_fetch_pag
     s->seed = 0x51u;
     s->fetch_cursor = 0;
     s->tenants.resize(cfg->n_tenants);
-    if (cfg->tenant_quota_pages) {
-        s->quota = cfg->tenant_quota_pages;
-    } else {
+    {
         uint64_t used = 0;
         if (pbm_pool_used(pool, &used, nullptr) != PBM_OK) { delete s; return PBM_ERR_CUDA; }
         const uint64_t cap = (uint64_t)(cfg->max_occupancy * (double)pool->n_pages);
-        s->quota = cap > used ? (cap - used) / cfg->n_tenants : 0;
+        s->budget = cap > used ? cap - used : 0;
     }
-    s->quota = std::min<uint64_t>(s->quota, cfg->ring_pages);
+    s->quota = cfg->tenant_quota_pages ? cfg->tenant_quota_pages : UINT64_MAX;
+    s->device_held = 0;
     const size_t ring_total = (size_t)cfg->n_tenants * cfg->ring_pages;
     bool ok = cudaMalloc(&s->d_rings, ring_total * sizeof(int32_t)) == cudaSuccess &&
               cudaMemset(s->d_rings, 0xff, ring_total * sizeof(int32_t)) == cudaSuccess &&
@@ -135,6 +150,7 @@ int pbm_server_create(pbm_pool* pool, pbm_bufmgr* bm, const int32_t* d_fetch_pag
 
 int pbm_server_destroy(pbm_server* s) {
     if (!s) return PBM_ERR_INVALID;
+    pbm::DeviceScope scope(s->pool->device);
     for (auto& b : s->slots) {
         if (b.stream) cudaStreamSynchronize(b.stream);
         if (b.stream) cudaStreamDestroy(b.stream);
@@ -152,6 +168,7 @@ int pbm_server_destroy(pbm_server* s) {
 int pbm_server_run(pbm_server* s, const pbm_request* reqs, uint64_t n, pbm_request_result* res,
                    pbm_server_report* report) {
     if (!s || (n && (!reqs || !res))) return PBM_ERR_INVALID;
+    pbm::DeviceScope scope(s->pool->device);
     for (uint64_t i = 0; i < n; ++i) {
         if (reqs[i].tenant >= s->cfg.n_tenants || reqs[i].op < PBM_REQ_ALLOC || reqs[i].op > PBM_REQ_FETCH)
             return PBM_ERR_INVALID;
@@ -165,7 +182,10 @@ int pbm_server_run(pbm_server* s, const pbm_request* reqs, uint64_t n, pbm_reque
     const auto t0 = Clock::now();
     auto now_s = [&]() { return std::chrono::duration<double>(Clock::now() - t0).count(); };
     uint64_t next = 0, finished = 0, batches = 0, in_flight = 0, max_in_flight = 0, batch_reqs = 0;
-    uint64_t pages_done = 0;
+    uint64_t pages_done = 0, waited = 0, idle_passes = 0;
+    std::vector<uint8_t> waited_flag(n, 0), free_sized(n, 0), fully_admitted(n, 0);
+    std::vector<uint32_t> parts_pending(n, 0);
+    std::vector<uint64_t> free_done(n, 0);
     const double give_up_s = (n ? reqs[n - 1].arrival_s : 0.0) + s->cfg.drain_timeout_s;
     uint32_t rr = 0;   // round-robin start tenant
     while (finished < n) {
@@ -183,9 +203,6 @@ int pbm_server_run(pbm_server* s, const pbm_request* reqs, uint64_t n, pbm_reque
             if (q != cudaSuccess) return PBM_ERR_CUDA;
             const double td = now_s();
             for (uint64_t r : b.reqs) {
-                res[r].done_s = td;
-                res[r].status = 0;
-                pages_done += res[r].pages;
                 Tenant& tn = s->tenants[reqs[r].tenant];
                 if (reqs[r].op == PBM_REQ_ALLOC) {
                     for (auto& p : tn.allocs) if (p.req == r) p.done = true;
@@ -194,8 +211,15 @@ int pbm_server_run(pbm_server* s, const pbm_request* reqs, uint64_t n, pbm_reque
                         tn.allocs.pop_front();
                     }
                 }
+                // a FREE split over several batches is done with its last part
+                if (--parts_pending[r] != 0 || !fully_admitted[r]) continue;
+                res[r].done_s = td;
+                res[r].status = 0;
+                pages_done += res[r].pages;
                 ++finished;
             }
+            s->device_held -= b.freed_pages;   // the batch's frees have landed
+            b.freed_pages = 0;
             b.reqs.clear();
             b.busy = false;
             --in_flight;
@@ -211,16 +235,32 @@ int pbm_server_run(pbm_server* s, const pbm_request* reqs, uint64_t n, pbm_reque
             for (uint32_t k = 0; k < s->cfg.n_tenants && nreq < s->cfg.max_batch_requests; ++k) {
                 const uint32_t ti = (rr + k) % s->cfg.n_tenants;
                 Tenant& tn = s->tenants[ti];
-                while (!tn.queue.empty() && nreq < s->cfg.max_batch_requests && ng + 2u <= s->max_groups) {
-                    const uint64_t r = tn.queue.front();
+                uint64_t virt = tn.logical;    // pages held after the earlier queued requests, in arrival order
+                bool alloc_waits = false;      // an earlier ALLOC of this tenant waits for memory
+                size_t qi = 0;
+                while (qi < tn.queue.size() && nreq < s->cfg.max_batch_requests && ng + 2u <= s->max_groups) {
+                    const uint64_t r = tn.queue[qi];
                     const pbm_request& q = reqs[r];
                     if (q.op == PBM_REQ_ALLOC) {
-                        if (tn.logical + q.count > s->quota) {   // over budget: rejected, not queued
+                        if (alloc_waits) {     // ALLOCs keep their order
+                            virt += q.count;
+                            ++qi;
+                            continue;
+                        }
+                        if (q.count > s->budget || q.count > R || q.count > s->quota) {   // can never fit
                             res[r].status = PBM_ERR_EXHAUSTED;
                             res[r].admit_s = res[r].done_s = ta;
                             res[r].pages = 0;
-                            tn.queue.pop_front();
+                            tn.queue.erase(tn.queue.begin() + (std::ptrdiff_t)qi);
                             ++finished;
+                            continue;
+                        }
+                        if (s->device_held + q.count > s->budget || tn.logical + q.count > R ||
+                            tn.logical + q.count > s->quota) {   // waits until frees land
+                            if (!waited_flag[r]) { waited_flag[r] = 1; ++waited; }
+                            alloc_waits = true;
+                            virt += q.count;
+                            ++qi;
                             continue;
                         }
                         const uint64_t pos = tn.tail % R;
@@ -230,29 +270,58 @@ int pbm_server_run(pbm_server* s, const pbm_request* reqs, uint64_t n, pbm_reque
                             slot->h_groups[ng++] = pbm_group{PBM_OP_ALLOC, (uint32_t)(q.count - first), (uint64_t)ti * R};
                         tn.tail += q.count;
                         tn.logical += q.count;
+                        virt += q.count;
+                        s->device_held += q.count;
                         tn.allocs.push_back(Pending{r, q.count, false});
                         res[r].pages = q.count;
+                        fully_admitted[r] = 1;
                     } else if (q.op == PBM_REQ_FREE) {
-                        const uint64_t k2 = std::min<uint64_t>(q.count, tn.logical);
-                        if (tn.completed - tn.head < k2) break;   // wait for the allocations it frees
-                        if (k2) {
-                            const uint64_t pos = tn.head % R;
-                            const uint64_t first = std::min<uint64_t>(k2, R - pos);
-                            slot->h_groups[ng++] = pbm_group{PBM_OP_FREE, (uint32_t)first, (uint64_t)ti * R + pos};
-                            if (k2 > first)
-                                slot->h_groups[ng++] = pbm_group{PBM_OP_FREE, (uint32_t)(k2 - first), (uint64_t)ti * R};
+                        // its size follows from the tenant's own earlier requests: fixed when first seen
+                        if (!free_sized[r]) {
+                            free_sized[r] = 1;
+                            res[r].pages = std::min<uint64_t>(q.count, virt);
                         }
-                        tn.head += k2;
-                        tn.logical -= k2;
-                        res[r].pages = k2;
+                        const uint64_t left = res[r].pages - free_done[r];
+                        virt -= left;
+                        // pages it may release now: held (older than any waiting ALLOC) and
+                        // allocated on the device; the rest waits for the ALLOCs that bring them
+                        const uint64_t part = std::min<uint64_t>(left, std::min<uint64_t>(tn.logical,
+                                                                                         tn.completed - tn.head));
+                        if (part) {
+                            const uint64_t pos = tn.head % R;
+                            const uint64_t first = std::min<uint64_t>(part, R - pos);
+                            slot->h_groups[ng++] = pbm_group{PBM_OP_FREE, (uint32_t)first, (uint64_t)ti * R + pos};
+                            if (part > first)
+                                slot->h_groups[ng++] = pbm_group{PBM_OP_FREE, (uint32_t)(part - first), (uint64_t)ti * R};
+                            tn.head += part;
+                            tn.logical -= part;
+                            free_done[r] += part;
+                            slot->freed_pages += part;
+                            if (res[r].admit_s == 0.0) res[r].admit_s = ta;
+                            slot->reqs.push_back(r);
+                            ++parts_pending[r];
+                            ++nreq;
+                        }
+                        if (free_done[r] < res[r].pages) break;   // the rest waits; so do later requests
+                        fully_admitted[r] = 1;
+                        if (!part) {   // nothing to release (a FREE of 0 pages): done with the batch
+                            if (res[r].admit_s == 0.0) res[r].admit_s = ta;
+                            slot->reqs.push_back(r);
+                            ++parts_pending[r];
+                            ++nreq;
+                        }
+                        tn.queue.erase(tn.queue.begin() + (std::ptrdiff_t)qi);
+                        continue;
                     } else {
                         if (fetch_pages + q.count > s->max_fetch) break;
                         fetch_pages += q.count;
                         res[r].pages = q.count;
+                        fully_admitted[r] = 1;
                     }
                     res[r].admit_s = ta;
                     slot->reqs.push_back(r);
-                    tn.queue.pop_front();
+                    ++parts_pending[r];
+                    tn.queue.erase(tn.queue.begin() + (std::ptrdiff_t)qi);
                     ++nreq;
                 }
             }
@@ -299,7 +368,14 @@ int pbm_server_run(pbm_server* s, const pbm_request* reqs, uint64_t n, pbm_reque
                 continue;
             }
         }
-        if (next >= n && in_flight == 0 && finished < n && now_s() > give_up_s) break;   // unadmittable leftovers
+        // nothing left to arrive, nothing in flight, and this pass admitted
+        // nothing: no later pass can admit anything either (stranded requests)
+        if (next >= n && in_flight == 0 && finished < n) {
+            ++idle_passes;
+            if (idle_passes > 1 || now_s() > give_up_s) break;
+        } else {
+            idle_passes = 0;
+        }
     }
     for (auto& b : s->slots) cudaStreamSynchronize(b.stream);
     if (report) {
@@ -327,12 +403,19 @@ int pbm_server_run(pbm_server* s, const pbm_request* reqs, uint64_t n, pbm_reque
         report->p50_s = pct(0.50);
         report->p99_s = pct(0.99);
         report->mean_batch_requests = batches ? (double)batch_reqs / (double)batches : 0.0;
+        report->waited = waited;
+        uint64_t stranded = 0;
+        for (uint64_t i = 0; i < n; ++i) stranded += res[i].status == -1;
+        report->stranded = stranded;
     }
-    return finished == n ? PBM_OK : PBM_ERR_TIMEOUT;
+    // stranded requests (nothing could ever admit them) end the run normally;
+    // only running out of drain_timeout_s with work still possible is a timeout
+    return (finished == n || idle_passes > 1) ? PBM_OK : PBM_ERR_TIMEOUT;
 }
 
 int pbm_server_tenant_pages(pbm_server* s, uint32_t tenant, int32_t* h_out, uint64_t max_out, uint64_t* h_n) {
     if (!s || tenant >= s->cfg.n_tenants || !h_n) return PBM_ERR_INVALID;
+    pbm::DeviceScope scope(s->pool->device);
     const Tenant& tn = s->tenants[tenant];
     const uint64_t k = tn.tail - tn.head;
     *h_n = k;

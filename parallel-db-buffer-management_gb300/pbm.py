@@ -56,7 +56,8 @@ class PoolConfig(Structure):
 class WalkConfig(Structure):
     _fields_ = [("strategy", c_int32), ("word_bits", c_int32), ("collab_width", c_int32),
                 ("stride", c_uint32), ("max_steps", c_uint32), ("block_size", c_int32),
-                ("blocks_per_sm", c_int32), ("free_merge", c_int32)]
+                ("blocks_per_sm", c_int32), ("free_merge", c_int32), ("fail_fast", c_int32),
+                ("reserved", c_int32)]
 
 
 class Group(Structure):
@@ -129,7 +130,8 @@ class MonitorSample(Structure):
 class ServerReport(Structure):
     _fields_ = [("requests", c_uint64), ("completed", c_uint64), ("rejected", c_uint64), ("pages", c_uint64),
                 ("batches", c_uint64), ("max_in_flight", c_uint64), ("wall_s", c_double), ("p50_s", c_double),
-                ("p99_s", c_double), ("mean_batch_requests", c_double)]
+                ("p99_s", c_double), ("mean_batch_requests", c_double), ("waited", c_uint64),
+                ("stranded", c_uint64)]
 
 
 # (name, restype, argtypes) -- every entry point of include/pbm.h
@@ -204,6 +206,7 @@ SIGNATURES = [
     ("pbm_bufmgr_check", c_int, [c_void_p, POINTER(BufMgrCheck), c_void_p]),
     ("pbm_bufmgr_frames", c_int, [c_void_p, POINTER(c_void_p), POINTER(c_size_t)]),
     ("pbm_bufmgr_gather", c_int, [c_void_p, c_void_p, c_uint32, c_uint32, c_void_p, c_void_p]),
+    ("pbm_bufmgr_read_tables", c_int, [c_void_p, c_void_p, c_void_p, c_void_p]),
     ("pbm_server_create", c_int, [c_void_p, c_void_p, c_void_p, c_uint64, POINTER(ServerConfig),
                                   POINTER(c_void_p)]),
     ("pbm_server_run", c_int, [c_void_p, POINTER(Request), c_uint64, POINTER(RequestResult), POINTER(ServerReport)]),
@@ -260,9 +263,9 @@ def _check(fn, rc, allow=()):
 
 
 def walk_config(strategy=COLLAB_RW_BM, word_bits=32, collab_width=32, stride=1, max_steps=4096,
-                block_size=256, blocks_per_sm=0, free_merge=0) -> WalkConfig:
+                block_size=256, blocks_per_sm=0, free_merge=0, fail_fast=0) -> WalkConfig:
     return WalkConfig(strategy, word_bits, collab_width, stride, max_steps, block_size, blocks_per_sm,
-                      free_merge)
+                      free_merge, fail_fast, 0)
 
 
 class Pool:
@@ -494,6 +497,7 @@ class BufferManager:
                  backing=None):
         self.lib = lib()
         cfg = BufMgrConfig(n_logical, n_frames, frame_size, policy, n_arms, max_sweep, 0)
+        self.n_logical, self.n_frames = n_logical, n_frames
         h = c_void_p()
         _check("pbm_bufmgr_create", self.lib.pbm_bufmgr_create(byref(cfg), _ptr(backing), byref(h)))
         self.h = h
@@ -519,6 +523,20 @@ class BufferManager:
     def gather(self, frame_ids, n, bytes_per_frame, out, stream=0):
         return _check("pbm_bufmgr_gather", self.lib.pbm_bufmgr_gather(self.h, _ptr(frame_ids), n, bytes_per_frame,
                                                                       _ptr(out), stream))
+
+    def read_tables(self, stream=0):
+        """(frame of each page (-1 not resident), pins of each page, reference
+        bit of each page, page of each frame (-1 empty)) as numpy arrays."""
+        import numpy as np
+
+        e = np.empty(self.n_logical, dtype=np.uint64)
+        fp = np.empty(self.n_frames, dtype=np.uint32)
+        _check("pbm_bufmgr_read_tables",
+               self.lib.pbm_bufmgr_read_tables(self.h, e.ctypes.data, fp.ctypes.data, stream))
+        frame = (e >> np.uint64(32)).astype(np.uint32).view(np.int32)
+        pins = (e & np.uint64(0x7fffffff)).astype(np.int64)
+        ref = ((e >> np.uint64(31)) & np.uint64(1)).astype(bool)
+        return frame, pins, ref, fp.view(np.int32)
 
     def frames(self):
         p, n = c_void_p(), c_size_t()

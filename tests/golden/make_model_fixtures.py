@@ -1,7 +1,7 @@
 """Generate model_predictions.json from the reference's theoretical_models.py.
 
-Run in a checkout that has the reference project next to it (path given as
-argv[1], default /root/reference).  The committed JSON pins
+Run in a checkout that has the reference project next to it: its root is
+argv[1], else $PBM_REFERENCE_ROOT, else /root/reference.  The committed JSON pins
 oracle/models.py, which restates those closed forms; the statistical tests
 use the restatement, so the reference itself is not needed to run them.
 """
@@ -9,7 +9,7 @@ import json
 import os
 import sys
 
-ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+ref = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("PBM_REFERENCE_ROOT", "/root/reference")
 sys.path.insert(0, ref)
 import theoretical_models as tm  # noqa: E402
 

@@ -99,6 +99,49 @@ def pp_caller(pbm_mod):
     return ctypes.CDLL(out_so)
 
 
+def _build_so(name, sources, extra=()):
+    os.makedirs(BUILD, exist_ok=True)
+    out_so = os.path.join(BUILD, name)
+    libdir = os.path.join(PKG, "lib")
+    cmd = (["nvcc", "-shared", "-Xcompiler", "-fPIC", "-O2", "-std=c++17",
+            "-gencode", "arch=compute_103a,code=sm_103a", "-I", os.path.join(ROOT, "include")] + list(extra)
+           + [os.path.join(ROOT, "tests", "caller", s) for s in sources]
+           + ["-o", out_so, "-L", libdir] + (["-lpbm_dropin"] if "-rdc=true" in extra else [])
+           + ["-lpbm", "-Xlinker", "-rpath", "-Xlinker", libdir])
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    assert r.returncode == 0, r.stdout + r.stderr
+    return ctypes.CDLL(out_so)
+
+
+def test_parallel_page_strategies_share_one_page_store(cuda, pbm_mod):
+    """pageAddress names the same page memory for all nine strategies: a
+    payload written for the first strategy's page survives initialising the
+    other eight, which add their maps but no second page store."""
+    lib = _build_so("libcaller_pp_store.so", ["pp_caller.cu"])
+    out = (ctypes.c_longlong * 3)()
+    assert lib.pp_shared_store(out) == 0
+    took, payload, store = list(out)
+    assert payload == 0x5A5A1234
+    assert took < store                     # eight more stores would be 8x this
+
+
+def test_parallel_page_rdc_two_units_share_one_pool(cuda, pbm_mod):
+    """The -rdc link form (libpbm_dropin.a, README.md:7-13 of the reference):
+    one translation unit takes pages, another checks their payloads and frees
+    them, and the shared map's free count returns to its start."""
+    import numpy as np
+
+    lib = _build_so("libcaller_rdc.so", ["pp_rdc_alloc.cu", "pp_rdc_free.cu"], ["-rdc=true"])
+    n = 20000
+    ids = np.zeros(n, dtype=np.int32)
+    out = (ctypes.c_longlong * 4)()
+    assert lib.rdc_run(n, ids.ctypes.data_as(ctypes.c_void_p), out) == 0
+    bad, f0, f1, f2 = list(out)
+    assert bad == 0
+    assert (ids >= 0).all() and np.unique(ids).size == n and (ids < 41_900_000).all()
+    assert f0 == 41_900_000 and f0 - f1 == n and f2 == f0
+
+
 @pytest.mark.parametrize("which", list(range(12)))
 def test_parallel_page_dropin(cuda, pp_caller, which):
     """Every strategy of the monolithic API, called from a caller's kernel:

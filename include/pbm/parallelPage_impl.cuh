@@ -42,7 +42,11 @@ static inline void pbm_pp_init(int k, bool fifo) {
     }
     if (pbm_pp_host[k].pool) return;   // initialised already
     pbm::dropin::DeviceState ds{};
-    if (!pbm::dropin::create_pool(TOTAL_N_PAGES, PAGE_SIZE, PBM_PP_SLOTS, fifo, &pbm_pp_host[k], &ds, false)) return;
+    // only the clustered walks and the distributed clock keep per-thread state
+    const bool slots = k == PBM_PP_CRW || k == PBM_PP_DC || k == PBM_PP_CRW_BM;
+    if (!pbm::dropin::create_pool(TOTAL_N_PAGES, PAGE_SIZE, slots ? PBM_PP_SLOTS : 32u, fifo, &pbm_pp_host[k], &ds,
+                                  false))
+        return;
     cudaMemcpyToSymbol(pbm_pp_dev, &ds, sizeof(ds), sizeof(ds) * (size_t)k);
 }
 

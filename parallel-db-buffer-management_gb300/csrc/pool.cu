@@ -418,9 +418,9 @@ int pbm_pool_create(const pbm_pool_config* cfg, pbm_pool** out) {
     const uint32_t nb_scan = (uint32_t)((p->view.n_words32 + 4095u) / 4096u) + 1u;
     p->prefix_cap = 0;
     // the budget pass: one block per 256 64-bit words, at most 4 per SM; its
-    // free list covers launches into a pool at least 75% full
+    // free list covers launches into a pool at least half full
     p->budget_blocks = (uint32_t)std::min<uint64_t>((uint64_t)sm_count() * 4u, std::max<uint64_t>(1u, (nw64 + 255u) / 256u));
-    p->free_list_cap = std::max<uint64_t>(1024u, cfg->n_pages / 4u);
+    p->free_list_cap = std::max<uint64_t>(1024u, cfg->n_pages / 2u);
     bool ok = cudaMalloc(&p->d_words, p->bitmap_bytes) == cudaSuccess &&
               cudaMalloc(&p->d_stats, sizeof(DevStats)) == cudaSuccess &&
               cudaMalloc(&p->d_cursors, sizeof(int32_t) * p->max_slots) == cudaSuccess &&

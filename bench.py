@@ -95,7 +95,7 @@ SUB_KEYS = {
                  "hbm_frac"),
     "cpu_baseline": ("value", "unit", "cores", "kind", "sample"),
     "clocks": ("sm_mhz", "sm_max_mhz", "reasons"),
-    "reference_cuda_build": ("collab_ops_s", "rwbasic_ops_s"),
+    "reference_cuda_build": ("collab_ops_s", "rwbasic_ops_s", "singleclock_ops_s", "distclock_ops_s"),
 }
 
 
@@ -282,7 +282,7 @@ def run_reference(args, rank):
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "reference_cuda_build": {w + "_ops_s": (ref_gpu.get(w) or {}).get("value")
-                                 for w in ("collab", "rwbasic")},
+                                 for w in ("collab", "rwbasic", "singleclock", "distclock")},
     }
     emit(line, {"reference_cuda_build": ref_gpu}, args.details)
     return 0
@@ -314,7 +314,19 @@ def reference_cuda_build(args):
         except Exception as e:  # noqa: BLE001
             out[walk] = {"unavailable": str(e)[:300]}
     out["walks"] = {"collab": "CollabRW_BM.cuh getPage/freePage (warp-collaborative, atomicExch of whole words)",
-                    "rwbasic": "RandomWalkBasic.cuh getPage/freePage (page probe on an int-per-page map)"}
+                    "rwbasic": "RandomWalkBasic.cuh getPage/freePage (page probe on an int-per-page map)",
+                    "singleclock": "parallelPage.cu getPageSingleClock/freePageSingleClock on its own "
+                                   "41,900,000-page pool",
+                    "distclock": "parallelPage.cu getPageDistClock/freePageDistClock on its own 41,900,000-page "
+                                 "pool (launches below its 10^6 arm slots)"}
+    if ref_timing.available_pp():
+        n_clk = min(args.steps, 20) + args.warmup
+        clk_counts = group_counts(n_clk).sum(axis=1)
+        for walk in ("singleclock", "distclock"):
+            try:
+                out[walk] = ref_timing.churn_clock(walk, OCCUPANCY, clk_counts, args.warmup, seed=PREFILL_SEED)
+            except Exception as e:  # noqa: BLE001
+                out[walk] = {"unavailable": str(e)[:300]}
     return out
 
 
@@ -758,6 +770,56 @@ def config_strategies(torch, pbm, stream, flush, occs=(0.5, 0.9), n=1 << 20, rep
     return out
 
 
+def config_clock_churn(torch, pbm, stream, flush, n_steps=20, warmup=5):
+    """This build's SingleClock and DistClock on the churn the reference's
+    clocks are timed on: a pool of the reference's fixed 41,900,000 pages
+    (parallelPage.cuh:3) at 90% occupancy (seed 2), steps of LogU group
+    counts (seed 4), each request freeing its arena slot's page and taking a
+    new one (one free launch and one claim launch per slice of the arena)."""
+    sh = stream.cuda_stream
+    T = 41_900_000
+    pool = pbm.Pool(T, 4096)
+    out = {"pool_pages": T, "occupancy": OCCUPANCY, "unit": "ops/s", "l2": "flushed before every step",
+           "steps": n_steps}
+    counts = group_counts(warmup + n_steps).sum(axis=1)
+    for name, strat in (("singleclock", pbm.SINGLE_CLOCK), ("distclock", pbm.DIST_CLOCK)):
+        pool.reset(sh)
+        pool.prefill(OCCUPANCY, PREFILL_SEED, sh)
+        words = pool.read_bitmap(sh)
+        held = np.nonzero(np.unpackbits(words.view(np.uint8), bitorder="little")[:T])[0].astype(np.int32)
+        np.random.default_rng(PREFILL_SEED).shuffle(held)
+        H = len(held)
+        arena = torch.from_numpy(held).cuda()
+        cfg = pbm.walk_config(strat)
+        off, t_ms, ops = 0, 0.0, 0
+        for s_i, n in enumerate(counts):
+            n = int(n)
+            flush.zero_()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            k0 = 0
+            while k0 < n:
+                k = min(n - k0, H - off)
+                sl = arena[off:off + k]
+                pool.free(cfg, k, sl, stream=sh)
+                pool.alloc(cfg, k, 7000 + s_i * 131 + k0, sl, stream=sh)
+                off = (off + k) % H
+                k0 += k
+            e1.record(stream)
+            e1.synchronize()
+            if s_i >= warmup:
+                t_ms += e0.elapsed_time(e1)
+                ops += 2 * n
+        chk = pool.check(arena, H, sh)
+        out[name] = {"value": ops / (t_ms * 1e-3), "ms_per_step": t_ms / n_steps,
+                     "invariants_ok": bool(chk.n_duplicates == 0 and chk.n_not_marked == 0
+                                           and chk.n_failed == 0 and chk.used_pages == H)}
+        del arena
+    pool.close()
+    return out
+
+
 def config_buffer_manager(torch, pbm, stream, flush, n_fetch=1 << 26, round_size=1 << 18):
     """2^22 frames x 4 KiB over 2^24 logical pages; 2^26 fetches Zipf(0.99)
     over a seed-3 permutation; each pin held Geometric(0.25) rounds."""
@@ -942,6 +1004,7 @@ def run_configs(args, torch, pbm, stream):
                                                                       cpu=not args.no_cpu_baseline)),
             ("occupancy_sweep", lambda: config_occupancy_sweep(torch, pbm, stream, flush)),
             ("strategies", lambda: config_strategies(torch, pbm, stream, flush)),
+            ("clock_churn_reference_pool", lambda: config_clock_churn(torch, pbm, stream, flush)),
             ("buffer_manager", lambda: config_buffer_manager(torch, pbm, stream, flush)),
             ("malloc", lambda: config_malloc(torch, pbm, stream, flush)),
             ("serving", lambda: config_serving(torch, pbm, stream))]
@@ -1174,7 +1237,8 @@ def main():
                     help="a small case of another kernel, for ncu (alloc also runs the free kernel)")
     ap.add_argument("--configs", default="all",
                     help="other workloads measured after the headline: all, none, or a comma list of "
-                         "claim_write_free_50pct,occupancy_sweep,strategies,buffer_manager,malloc,serving")
+                         "claim_write_free_50pct,occupancy_sweep,strategies,clock_churn_reference_pool,"
+                         "buffer_manager,malloc,serving")
     ap.add_argument("--details", default=None,
                     help="also write the headline and every workload's results as one JSON file here")
     args = ap.parse_args()

@@ -2,14 +2,21 @@
 // KernelMallocSimple and KernelMallocCollab with host constructors and
 // device malloc(int) / free(void*), passed by value into a caller's kernels.
 //
-// All three share the size-classed allocator of pbm/pbm_malloc.cuh over a
-// pool of PBM_MALLOC_POOL_PAGES pages of PBM_MALLOC_PAGE_SIZE bytes (power of
-// two, 2 KiB .. 64 KiB; the reference's 264-byte pages cannot hold its own
-// 64 KiB-class chunks).  Differences from the reference, by design: free()
-// releases memory (KernelMallocSimple::free is empty in the reference,
-// malloc.cu:157-159, and KernelMallocCollab frees only whole chunks,
-// malloc.cu:300-320); the destructor leaves the pool alive because kernel
-// arguments are copies of the object -- call release() to free it.
+// All three allocate from one pool of PBM_MALLOC_POOL_PAGES pages of
+// PBM_MALLOC_PAGE_SIZE bytes (power of two, 2 KiB .. 64 KiB; the reference's
+// 264-byte pages cannot hold its own 64 KiB-class chunks), each run of pages
+// carrying a live-block count:
+//   * MemoryManager and KernelMallocCollab: the lanes of a warp pack their
+//     sub-page requests into one shared run, larger requests get runs of
+//     their own (pbm/pbm_malloc.cuh; the reference's warp suffix sum,
+//     malloc.cu:223-289);
+//   * KernelMallocSimple: each thread bumps through a chunk of its own and
+//     claims a new one when the next request does not fit (malloc.cu:100-152).
+// Differences from the reference, by design: free() releases memory
+// (KernelMallocSimple::free is empty in the reference, malloc.cu:157-159,
+// and KernelMallocCollab frees only whole chunks, malloc.cu:300-320); the
+// destructor leaves the pool alive because kernel arguments are copies of the
+// object -- call release() to free it.
 #pragma once
 #include <climits>
 
@@ -93,13 +100,97 @@ public:
     pbm_pool* m_pool;
 };
 
-/* KernelMallocSimple(maxNThreads): malloc.cuh:14-24, malloc.cu:61-160 */
+/* KernelMallocSimple(maxNThreads): malloc.cuh:14-24, malloc.cu:61-160.
+ * Each thread (global id below maxNThreads) keeps a chunk -- a run of pages
+ * -- and bumps through it: a malloc that fits the rest of the chunk takes its
+ * next bytes (16-byte aligned); one that does not retires the chunk and
+ * claims a new run just large enough for the request (malloc.cu:100-152),
+ * whose leftover serves the thread's next small requests.  Every block counts
+ * as live in its run and the thread's hold on its current chunk counts once
+ * more, so a run goes back to the pool when its last block is freed and its
+ * thread has moved on to another chunk or called retire(). */
 class KernelMallocSimple : public MemoryManager {
 public:
-    __host__ KernelMallocSimple(int _maxNThreads) : MemoryManager(_maxNThreads) {}
+    __host__ KernelMallocSimple(int _maxNThreads) : MemoryManager(_maxNThreads) {
+        m_threads = _maxNThreads > 0 ? _maxNThreads : 0;
+        m_chunk = nullptr;
+        if (m_pool && m_threads) {
+            if (cudaMalloc(&m_chunk, sizeof(int2) * (size_t)m_threads) != cudaSuccess) {
+                cudaGetLastError();
+                m_chunk = nullptr;
+            } else {
+                clear_chunks();
+            }
+        }
+    }
+    /* reset(): free all memory (malloc.cu:82-86) */
+    __host__ void reset() {
+        MemoryManager::reset();
+        clear_chunks();
+    }
+    __host__ void release() {
+        cudaFree(m_chunk);
+        m_chunk = nullptr;
+        MemoryManager::release();
+    }
+    /* malloc(size): nullptr on failure, for a thread at or past maxNThreads,
+     * or for a request above 255 pages */
+    __device__ void* malloc(int size) {
+        if (!m_view.start_of || !m_chunk || size <= 0) return nullptr;
+        const uint32_t tid = pbm::dropin::global_tid();
+        if (tid >= (uint32_t)m_threads) return nullptr;
+        const int2 st = m_chunk[tid];   // x: first page of the chunk (-1 none), y: bytes handed out
+        const uint32_t bytes = ((uint32_t)size + 15u) & ~15u;
+        const uint32_t page = m_view.pool.page_size;
+        if (st.x >= 0) {
+            const uint32_t cap = (uint32_t)m_view.len_of[st.x] * page;
+            if ((uint32_t)st.y + bytes <= cap) {
+                atomicAdd(m_view.live + st.x, 1);
+                m_chunk[tid] = make_int2(st.x, st.y + (int)bytes);
+                return m_view.pool.base + ((size_t)(uint32_t)st.x << m_view.page_shift) + st.y;
+            }
+            drop_chunk(st.x);
+        }
+        m_chunk[tid] = make_int2(-1, 0);
+        const uint32_t n = (bytes + page - 1u) / page;
+        if (n > 255u) return nullptr;
+        int32_t steps = 0;
+        const int32_t start = pbm::walk_span(m_view.pool, n, pbm::dropin::call_seed(), PBM_DROPIN_MAX_STEPS, &steps);
+        if (start < 0) return nullptr;
+        pbm::malloc_mark_run(m_view, start, n, 2);   // the block, and the thread's hold on its chunk
+        m_chunk[tid] = make_int2(start, (int)bytes);
+        return m_view.pool.base + ((size_t)(uint32_t)start << m_view.page_shift);
+    }
+    /* free(addr): the block's run loses one live block; the calling lanes
+     * must be converged */
+    __device__ void free(void* addr) { MemoryManager::free(addr); }
+    /* retire(): the calling thread lets go of its current chunk, which goes
+     * back to the pool once its blocks are freed (no reference counterpart) */
+    __device__ void retire() {
+        if (!m_chunk) return;
+        const uint32_t tid = pbm::dropin::global_tid();
+        if (tid >= (uint32_t)m_threads) return;
+        const int2 st = m_chunk[tid];
+        if (st.x >= 0) drop_chunk(st.x);
+        m_chunk[tid] = make_int2(-1, 0);
+    }
+    int m_threads;
+    int2* m_chunk;   // per thread: first page of its chunk and the bytes handed out
+
+private:
+    __device__ void drop_chunk(int32_t start) {
+        if (atomicSub(m_view.live + start, 1) == 1) pbm::free_span(m_view.pool, start, m_view.len_of[start]);
+    }
+    __host__ void clear_chunks() {
+        if (m_chunk) cudaMemset(m_chunk, 0xff, sizeof(int2) * (size_t)m_threads);   // no chunk
+        cudaDeviceSynchronize();
+    }
 };
 
-/* KernelMallocCollab(): malloc.cuh:27-37, malloc.cu:201-320 */
+/* KernelMallocCollab(): malloc.cuh:27-37, malloc.cu:201-320.  The lanes of
+ * a warp pack their sub-page requests into one shared run (largest class
+ * first, so each block is aligned to its class); requests of a page or more
+ * get runs of their own.  A run goes back to the pool with its last block. */
 class KernelMallocCollab : public MemoryManager {
 public:
     __host__ KernelMallocCollab() : MemoryManager() {}

@@ -51,3 +51,33 @@ extern "C" __global__ void fx_ll_seq(int n, const int* ops, int* out) {
         else { freePageLinkedList(ops[k], nullptr); out[k] = -1; }
     }
 }
+
+// ---- churn for timing (reference timing arm) ----
+// Thread i releases the page held in arena slot (off + i) mod H with the
+// strategy's own freePage, then takes a new one with its getPage and stores
+// it in the slot.  Releasing first keeps the free pages at or above their
+// start, so the unbounded getPage loops always have pages to find while the
+// caller keeps each launch well below the free pages.
+extern "C" __global__ void fx_churn_sc(int n, int* arena, int H, int off) {
+    const int i = fx_tid();
+    if (i >= n) return;
+    int slot = off + i;
+    if (slot >= H) slot -= H;
+    freePageSingleClock(arena[slot], nullptr);
+    arena[slot] = getPageSingleClock(nullptr);
+}
+
+// DistClock indexes its arms by the global thread id, so a launch must stay
+// below MAX_THREADS_DISTCLOCK threads (the caller caps it).
+extern "C" __global__ void fx_churn_dc(int n, int* arena, int H, int off) {
+    const int i = fx_tid();
+    if (i >= n) return;
+    int slot = off + i;
+    if (slot >= H) slot -= H;
+    freePageDistClock(arena[slot], nullptr);
+    arena[slot] = getPageDistClock(nullptr);
+}
+
+// The single clock's arm (an int that must stay far from 2^31) and the
+// distributed clock's thread limit.
+extern "C" __global__ void fx_sc_arm(int* out) { out[0] = d_SingleClockArm; out[1] = MAX_THREADS_DISTCLOCK; }

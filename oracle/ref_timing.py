@@ -130,3 +130,91 @@ def churn(words: np.ndarray, n_pages: int, held: np.ndarray, step_counts, warmup
         "used_before": used0,
         "used_after": int(bits.sum()),
     }
+
+
+def available_pp() -> bool:
+    return have_cubin("ref_pp.cubin")
+
+
+def churn_clock(walk: str, occupancy: float, step_counts, warmup: int, seed: int = 2,
+                flush_bytes: int = 512 << 20, max_launch: int = 1 << 19, block: int = 256, arm_seed: int = 11):
+    """Churn of the reference's SingleClock or DistClock (parallelPage.cu:491-509,
+    571-592) on its own pool of TOTAL_N_PAGES pages (fixed at compile time,
+    41,900,000), prefilled Bernoulli(occupancy) with `seed`; each request
+    frees its arena slot's page and takes a new one (fx_churn_sc / _dc).
+
+    Safety: releasing first keeps the free pages at or above their start and
+    no launch asks for more than half of them; DistClock launches stay below
+    its MAX_THREADS_DISTCLOCK arm slots (its arms are indexed by thread id);
+    the single clock's int arm is read after every step and the run stops
+    long before it could pass 2^31 (parallelPage.cu:498-499 would then index
+    before the map).  DistClock's arms start at uniform random pages drawn on
+    the host (the reference draws them from clock() in randomizeArmDistClock)."""
+    import oracle
+
+    assert walk in ("singleclock", "distclock")
+    drv = Driver()
+    mod = drv.module("ref_pp.cubin")
+    info = drv.upload(np.zeros(2, np.int32))
+    drv.launch(drv.fn(mod, "fx_total_pages"), 1, 1, D(info))
+    T = int(drv.d2h(np.zeros(2, np.int32), info)[0])
+    words = oracle.bernoulli_bitmap(T, occupancy, seed)
+    bits = np.unpackbits(words.view(np.uint8), bitorder="little")[:T]
+    held = np.nonzero(bits)[0].astype(np.int32)
+    np.random.default_rng(seed).shuffle(held)
+    H = int(held.size)
+    free0 = T - H
+    d_map = drv.upload(bits.astype(np.int32))
+    del bits
+    arm_info = drv.upload(np.zeros(2, np.int32))
+    drv.launch(drv.fn(mod, "fx_sc_arm"), 1, 1, D(arm_info))
+    max_dc = int(drv.d2h(np.zeros(2, np.int32), arm_info)[1])
+    arms = np.random.default_rng(arm_seed).integers(0, T, size=max_dc).astype(np.int32)
+    d_arms = drv.upload(arms)
+    d_dummy = drv.alloc(1 << 20)
+    drv.launch(drv.fn(mod, "fx_setup"), 1, 1, D(d_map), D(d_map), D(d_arms), D(d_dummy), D(d_dummy))
+    cap = int(min(max_launch, free0 // 2, max_dc if walk == "distclock" else max_launch))
+    f = drv.fn(mod, "fx_churn_sc" if walk == "singleclock" else "fx_churn_dc")
+    f_arm = drv.fn(mod, "fx_sc_arm")
+    d_arena = drv.upload(held)
+    d_flush = drv.alloc(flush_bytes)
+    ev = [(drv.event(), drv.event()) for _ in step_counts]
+    off, done_steps, stopped, arm = 0, 0, None, 0
+    for s, n in enumerate(step_counts):
+        n = int(n)
+        drv.memset8(d_flush, s & 0xFF, flush_bytes)
+        e0, e1 = ev[s]
+        drv.record(e0)
+        k0 = 0
+        while k0 < n:
+            k = min(cap, n - k0)
+            drv.launch_async(f, (k + block - 1) // block, block, k, D(d_arena), H, off)
+            off = (off + k) % H
+            k0 += k
+        drv.record(e1)
+        drv.sync()
+        done_steps = s + 1
+        if walk == "singleclock":
+            drv.launch(f_arm, 1, 1, D(arm_info))
+            arm = int(drv.d2h(np.zeros(2, np.int32), arm_info)[0])
+            if arm < 0 or arm > 1_500_000_000:
+                stopped = f"single-clock arm at {arm} after step {s}"
+                break
+    ms = [drv.elapsed_ms(e0, e1) for e0, e1 in ev[warmup:done_steps]]
+    reqs = [int(c) for c in list(step_counts)[warmup:done_steps]]
+    m = drv.d2h(np.empty(T, np.int32), d_map)
+    arena = drv.d2h(np.empty(H, np.int32), d_arena)
+    ok = (arena >= 0) & (arena < T)
+    u, c = np.unique(arena[ok], return_counts=True)
+    for e0, e1 in ev:
+        drv.destroy_event(e0)
+        drv.destroy_event(e1)
+    drv.free_all()
+    t = sum(ms)
+    return {
+        "value": 2.0 * sum(reqs) / (t * 1e-3) if t > 0 else None, "unit": "ops/s",
+        "pool_pages": T, "occupancy": occupancy, "steps_timed": len(ms), "ms_per_step": t / max(1, len(ms)),
+        "requests_timed": sum(reqs), "launch_cap": cap, "stopped": stopped, "final_arm": arm,
+        "bad_ids": int((~ok).sum()), "ids_held_twice": int((c > 1).sum()),
+        "used_before": H, "used_after": int(np.count_nonzero(m)),
+    }

@@ -204,7 +204,9 @@ __global__ void __launch_bounds__(256, MINB) k_batch_persistent(BatchArgs a, con
     const unsigned long long per_block = (n_chunks + gridDim.x - 1ull) / gridDim.x;
     const unsigned long long c_begin = (unsigned long long)blockIdx.x * per_block;
     const unsigned long long c_end = min(n_chunks, c_begin + per_block);
-    uint32_t g_lo = 0;                 // group of the warp's previous chunk (chunks only grow)
+    // the group of the warp's previous chunk: chunks only grow and a group
+    // spans many chunks, so a chunk that still lies in it skips the search
+    uint32_t g0 = 0;
     for (;;) {
         uint32_t k = 0;
         if (lane == 0) k = atomicAdd(&s_next_chunk, 1u);
@@ -212,8 +214,7 @@ __global__ void __launch_bounds__(256, MINB) k_batch_persistent(BatchArgs a, con
         const unsigned long long chunk = c_begin + k;
         if (chunk >= c_end) break;
         const unsigned long long q0 = chunk * CH;
-        const uint32_t g0 = find_group_warp(pre, a.n_groups, q0, g_lo);
-        g_lo = g0;
+        if (q0 >= pre[g0 + 1u]) g0 = find_group_warp(pre, a.n_groups, q0, g0);
         const unsigned long long g0_end = pre[g0 + 1u];
         // a chunk usually lies inside one group; requests past its end search on
         auto locate = [&](unsigned long long q, int& op, unsigned long long& slot) {

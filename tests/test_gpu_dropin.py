@@ -188,3 +188,18 @@ def test_malloc_classes_dropin(cuda, pbm_mod, which):
     assert lib.malloc_run(which, 20000, out) == 0
     bad, f0, f1, f2 = list(out)
     assert bad == 0 and f1 < f0 and f2 == f0
+
+
+def test_malloc_simple_bumps_through_a_chunk_per_thread(cuda, pbm_mod):
+    """KernelMallocSimple is the reference's per-thread chunk allocator
+    (malloc.cu:100-152): a thread's small mallocs are consecutive slices of
+    its own chunk (one page per thread here), and freeing them plus retire()
+    gives every page back."""
+    lib = _build_so("libcaller_malloc_bump.so", ["malloc_caller.cu"])
+    out = (ctypes.c_longlong * 4)()
+    n = 20000
+    assert lib.malloc_bump_run(n, out) == 0
+    bad, f0, f1, f2 = list(out)
+    assert bad == 0
+    assert abs((f0 - f1) / 1e6 * (1 << 18) - n) < 2     # one page per thread
+    assert f2 == f0

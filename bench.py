@@ -1098,6 +1098,68 @@ def run_profile_kernel(args):
         st = pool.stats(sh)
         out.update(successes=st.successes, failures=st.failures, frees=st.frees)
         pool.close()
+    elif args.profile_kernel == "catalog":
+        # every kernel of the library once, for single-kernel captures (-k
+        # NAME -c 1): a 2^24-page pool at 50% for the walks (2^22 requests),
+        # frees, runs, the fail-fast budget pass, the checks, the free list,
+        # the monitor's popcount and one plain batch launch
+        import ctypes
+
+        N = 1 << 22
+        ids = torch.empty(N, dtype=torch.int32, device="cuda")
+        pool = pbm.Pool(T_PAGES, PAGE_SIZE, max_slots=N)
+        for strat in (pbm.RANDOM_WALK, pbm.RANDOM_WALK_BM, pbm.CLUSTERED_RW_BM, pbm.SINGLE_CLOCK, pbm.DIST_CLOCK,
+                      pbm.COLLAB_RW_BM, pbm.LINKED_LIST):
+            pool.reset(sh)
+            pool.prefill(0.5, PREFILL_SEED, sh)
+            cfg = pbm.walk_config(strat)
+            flush.zero_()
+            pool.alloc(cfg, N, 70 + strat, ids, stream=sh)
+            flush.zero_()
+            pool.free(cfg, N, ids, stream=sh)
+        pool.used(sh)
+        # fail-fast: a launch asking for more pages than are free (budget pass + free list)
+        pool.reset(sh)
+        pool.prefill(0.95, PREFILL_SEED, sh)
+        flush.zero_()
+        pool.alloc(pbm.walk_config(pbm.COLLAB_RW_BM, fail_fast=1), N, 80, ids, stream=sh)
+        chk = pool.check(ids, N, sh)
+        # runs across words, and their frees
+        pool.reset(sh)
+        pool.prefill(0.05, PREFILL_SEED, sh)
+        R = 1 << 18
+        k = torch.from_numpy(np.random.default_rng(1).integers(1, 65, R).astype(np.int32)).cuda()
+        flush.zero_()
+        pool.alloc_spans(R, k, 81, ids[:R], max_steps=256, stream=sh)
+        flush.zero_()
+        pool.free_runs(R, ids[:R], k, stream=sh)
+        # the no-alloc check on a pool at its 2^23-page limit
+        small = pbm.Pool(1 << 23, PAGE_SIZE)
+        small.prefill(0.5, 3, sh)
+        small.alloc(pbm.walk_config(pbm.COLLAB_RW_BM), 1 << 20, 82, ids[:1 << 20], stream=sh)
+        res = pbm.CheckResult()
+        pbm.lib().pbm_check_ids_noalloc(small.bitmap_ptr, small.n_pages, ids.data_ptr(), 1 << 20, ctypes.byref(res),
+                                        sh)
+        # the monitor's popcount beside nothing else
+        mon = pbm.Monitor(small, interval_us=1000, max_samples=2)
+        time.sleep(0.05)
+        mon.stop()
+        small.close()
+        # one plain batch launch of the benchmark's walk (a 65,536-request swap group)
+        pool.reset(sh)
+        pool.prefill(OCCUPANCY, PREFILL_SEED, sh)
+        words = pool.read_bitmap(sh)
+        held = np.nonzero(np.unpackbits(words.view(np.uint8), bitorder="little")[:T_PAGES])[0].astype(np.int32)
+        arena = torch.from_numpy(held).cuda()
+        flush.zero_()
+        pool.batch(named_walk(pbm, "pair32c"), None, pbm.groups_array([(pbm.OP_SWAP, 65536, 0)]), 1, arena,
+                   len(held), 83, pbm.LAUNCH_PLAIN, stream=sh)
+        torch.cuda.synchronize()
+        out.update(used=pool.used(sh), fail_fast_ok=int(chk.n_ok), noalloc_ok=int(res.n_ok))
+        pool.close()
+        # the roofline's ceiling kernel, captured the same way
+        pbm.atomic_ceiling(words=1 << 22, threads=pbm_sms() * 2048, iters=64, returning=1, pattern=2)
+        torch.cuda.synchronize()
     elif args.profile_kernel == "misc":
         # one launch each: page-probe and word-probe walks (2^22 claims at 50%),
         # runs across words (2^18 runs of 1..64 pages at 5%), config 1's
@@ -1233,7 +1295,7 @@ def main():
                          "frees unmerged (the autotuner's pick at 90%%)")
     ap.add_argument("--walk", default="auto", choices=("auto",) + WALKS,
                     help="auto: the autotuner picks (untimed, before the timed steps); else a fixed walk")
-    ap.add_argument("--profile-kernel", default=None, choices=["bufmgr", "malloc", "alloc", "misc"],
+    ap.add_argument("--profile-kernel", default=None, choices=["bufmgr", "malloc", "alloc", "misc", "catalog"],
                     help="a small case of another kernel, for ncu (alloc also runs the free kernel)")
     ap.add_argument("--configs", default="all",
                     help="other workloads measured after the headline: all, none, or a comma list of "

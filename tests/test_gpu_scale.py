@@ -238,3 +238,84 @@ def test_config3_buffer_manager_at_size_checked_on_the_host(cuda, pbm_mod, orc, 
     assert evicting and c.evictions > 0 and c.failures == 0 and c.timeouts == 0 and c.bad_unpins == 0
     assert c.hits + c.misses == R * rounds
     bm.close()
+
+
+def test_config4_malloc_round_on_the_32gib_pool(cuda, pbm_mod, orc):
+    """Config 4 at its own size: a 32 GiB pool of 4 KiB pages, 256 caller
+    groups with LogU[1, 65536] requests (seed 4) and sizes LogU[16 B, 64 KiB]
+    in one persistent launch; then a uniformly random 50% of the blocks
+    freed and a second round of mallocs.  On the host: every live block
+    (survivors and new ones together) is aligned to its class (or a page),
+    inside the pool and disjoint from every other; freeing everything leaves
+    an empty bitmap, no live run and no bad free."""
+    import math
+
+    torch = cuda
+    pbm = pbm_mod
+    T, PAGE = 1 << 23, 4096
+    pool = pbm.Pool(T, PAGE, materialize=True)
+    pool.malloc_init()
+    rng = np.random.default_rng(4)
+    DT = np.dtype([("op", "<i4"), ("count", "<u4"), ("offset", "<u8")])
+
+    def logu_counts(n):
+        return np.clip(np.floor(np.exp(rng.uniform(0.0, math.log(65537), n))), 1, 65536).astype(np.int64)
+
+    def logu_sizes(n):
+        return np.clip(np.exp(rng.uniform(math.log(16), math.log(65536), n)), 16, 65536).astype(np.uint32)
+
+    c1, c2 = logu_counts(256), logu_counts(256)
+    n1, n2 = int(c1.sum()), int(c2.sum())
+    k = n1 // 2
+    slots = n1 + k + n2
+    sizes = np.zeros(slots, dtype=np.uint32)
+    sizes[:n1] = logu_sizes(n1)
+    sizes[n1 + k:] = logu_sizes(n2)
+    d_sizes = torch.from_numpy(sizes.astype(np.int32)).cuda()
+    ptrs = torch.zeros(slots, dtype=torch.int64, device="cuda")
+
+    def launch(groups, seed):
+        tab = np.zeros(len(groups), dtype=DT)
+        for i, g in enumerate(groups):
+            tab[i] = g
+        pool.malloc_batch(torch.from_numpy(tab.view(np.uint8).copy()).cuda(), None, len(groups), d_sizes, ptrs,
+                          slots, seed, pbm.LAUNCH_PERSISTENT, max_steps=512)
+        torch.cuda.synchronize()
+
+    def check(live_ptrs, live_sizes):
+        ok = live_ptrs != 0
+        off = live_ptrs[ok] - pool.base_ptr
+        cb = np.maximum(16, 1 << np.ceil(np.log2(np.maximum(live_sizes[ok].astype(np.int64), 1))).astype(np.int64))
+        assert (off % np.minimum(cb, PAGE) == 0).all()
+        assert (off >= 0).all() and ((off + cb) <= T * PAGE).all()
+        order = np.argsort(off)
+        s, e = off[order], (off + cb)[order]
+        assert (s[1:] >= e[:-1]).all()
+        return int(ok.sum())
+
+    offs1 = np.concatenate([[0], np.cumsum(c1)[:-1]])
+    launch([(pbm.OP_MALLOC, int(c), int(o)) for c, o in zip(c1, offs1)], 41)
+    p1 = ptrs.cpu().numpy()[:n1].copy()
+    assert check(p1, sizes[:n1]) >= int(0.99 * n1)          # the first round fits the empty pool
+    # free a uniform half: their pointers move to slots [n1, n1 + k)
+    perm = rng.permutation(n1)
+    gone, kept = perm[:k], perm[k:]
+    ptrs[n1:n1 + k].copy_(torch.from_numpy(p1[gone]))
+    launch([(pbm.OP_MFREE, k, n1)], 42)
+    assert (ptrs[n1:n1 + k].cpu().numpy() == 0).all()
+    offs2 = n1 + k + np.concatenate([[0], np.cumsum(c2)[:-1]])
+    launch([(pbm.OP_MALLOC, int(c), int(o)) for c, o in zip(c2, offs2)], 43)
+    p2 = ptrs.cpu().numpy()[n1 + k:].copy()
+    live = np.concatenate([p1[kept], p2])
+    live_sizes = np.concatenate([sizes[:n1][kept], sizes[n1 + k:]])
+    check(live, live_sizes)
+    live_runs, bad = pool.malloc_counts()
+    assert bad == 0 and live_runs > 0
+    # free everything that is live: the pool comes back empty
+    nl = live.size
+    ptrs[:nl].copy_(torch.from_numpy(live))
+    launch([(pbm.OP_MFREE, nl, 0)], 44)
+    live_runs, bad = pool.malloc_counts()
+    assert live_runs == 0 and bad == 0
+    assert pool.used() == 0
+    pool.close()

@@ -790,7 +790,11 @@ def config_clock_churn(torch, pbm, stream, flush, n_steps=20, warmup=5):
         np.random.default_rng(PREFILL_SEED).shuffle(held)
         H = len(held)
         arena = torch.from_numpy(held).cuda()
-        cfg = pbm.walk_config(strat)
+        # the reference's clocks search without a bound; 2^20 steps keeps this
+        # build's bounded sweep from giving up where an arm crosses a long run
+        # of held pages
+        cfg = pbm.walk_config(strat, max_steps=1 << 20)
+        st0 = pool.stats(sh)
         off, t_ms, ops = 0, 0.0, 0
         for s_i, n in enumerate(counts):
             n = int(n)
@@ -812,7 +816,11 @@ def config_clock_churn(torch, pbm, stream, flush, n_steps=20, warmup=5):
                 t_ms += e0.elapsed_time(e1)
                 ops += 2 * n
         chk = pool.check(arena, H, sh)
+        st1 = pool.stats(sh)
         out[name] = {"value": ops / (t_ms * 1e-3), "ms_per_step": t_ms / n_steps,
+                     "failures": int(st1.failures - st0.failures),
+                     "mean_steps": (st1.steps - st0.steps) / max(1, st1.successes + st1.failures - st0.successes
+                                                                  - st0.failures),
                      "invariants_ok": bool(chk.n_duplicates == 0 and chk.n_not_marked == 0
                                            and chk.n_failed == 0 and chk.used_pages == H)}
         del arena

@@ -388,7 +388,7 @@ def run_ours(args, rank, world, local_rank):
     tuned = []
     if args.walk == "auto":
         tuned = pool.autotune(d_tab[:N_GROUPS * 16], N_GROUPS, int(counts[0].sum()), arena, H, seed=SEED0 - 999,
-                              reps=4, stream=sh)
+                              reps=7, stream=sh)
         torch.cuda.synchronize()
     cfg = named_walk(pbm, "collab32c" if args.walk == "auto" else args.walk)
     if tuned:

@@ -312,12 +312,14 @@ int pbm_qmalloc_counts(pbm_pool *pool, uint64_t *h_queued, uint64_t *h_chunks, u
  * 8/16/32, 32/64-bit words, stride, blocks per SM, merged frees -- once
  * untimed and then `reps` times, each timed alone after an L2 flush (a
  * 256 MiB device scratch, allocated for the call), ranked by the median
- * (ms_per_batch), and returns up to max_out results sorted fastest first.
- * Swaps keep the pool's occupancy, so tune once per occupancy band. */
+ * (ms_per_batch) and, where medians tie (event timings are quantised), by
+ * the mean (ms_mean); candidates that tie on both keep the candidate order.
+ * Returns up to max_out results sorted fastest first.  Swaps keep the pool's
+ * occupancy, so tune once per occupancy band. */
 typedef struct {
     pbm_walk_config cfg;
-    float ms_per_batch;
-    float reserved;
+    float ms_per_batch;    /* median of the reps */
+    float ms_mean;         /* mean of the reps */
     double ops_per_s;      /* 2 * requests / time (one alloc + one free each) */
 } pbm_tune_result;
 int pbm_autotune(pbm_pool *pool, const pbm_group *d_groups, uint32_t n_groups, uint64_t requests,

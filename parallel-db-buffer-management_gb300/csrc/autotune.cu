@@ -9,7 +9,9 @@
 // the persistent kernel once untimed and then `reps` times, each timed alone
 // with CUDA events after the L2 is flushed (a 256 MiB write, twice the L2), as
 // a batch that arrives after other work would find it; the median time
-// ranks the candidate.  A swap frees one page for every page it takes, so the
+// ranks the candidate, the mean breaks ties between equal medians (event
+// times are quantised, so close candidates often share a median), and a
+// stable sort keeps the candidate order where both tie.  A swap frees one page for every page it takes, so the
 // pool stays in its occupancy band while it is tuned.  The
 // caller tunes once per band (e.g. after prefilling to 50/75/90/95%) and keeps
 // the winning configuration per band.
@@ -115,19 +117,24 @@ extern "C" int pbm_autotune(pbm_pool* pool, const pbm_group* d_groups, uint32_t 
                 rc = PBM_ERR_CUDA;
         }
         if (rc) break;
+        double sum = 0.0;
+        for (float x : times) sum += x;
         std::sort(times.begin(), times.end());
         const float ms = times[(size_t)reps / 2];
         pbm_tune_result t{};
         t.cfg = c;
         t.ms_per_batch = ms;
+        t.ms_mean = (float)(sum / reps);
         t.ops_per_s = ms > 0.f ? 2.0 * (double)requests / (ms * 1e-3) : 0.0;
         res.push_back(t);
     }
     if (rc == PBM_ERR_CUDA) cudaGetLastError();
     cleanup();
     if (rc) return rc;
-    std::sort(res.begin(), res.end(),
-              [](const pbm_tune_result& a, const pbm_tune_result& b) { return a.ops_per_s > b.ops_per_s; });
+    std::stable_sort(res.begin(), res.end(), [](const pbm_tune_result& a, const pbm_tune_result& b) {
+        if (a.ms_per_batch != b.ms_per_batch) return a.ms_per_batch < b.ms_per_batch;
+        return a.ms_mean < b.ms_mean;
+    });
     const uint32_t n = (uint32_t)std::min<size_t>(res.size(), max_out);
     for (uint32_t i = 0; i < n; ++i) h_out[i] = res[i];
     *h_n_out = n;

@@ -85,7 +85,7 @@ BM_SINGLE_CLOCK, BM_DIST_CLOCK = 0, 1
 
 
 class TuneResult(Structure):
-    _fields_ = [("cfg", WalkConfig), ("ms_per_batch", ctypes.c_float), ("reserved", ctypes.c_float),
+    _fields_ = [("cfg", WalkConfig), ("ms_per_batch", ctypes.c_float), ("ms_mean", ctypes.c_float),
                 ("ops_per_s", c_double)]
 
 

@@ -845,30 +845,42 @@ def config_buffer_manager(torch, pbm, stream, flush, n_fetch=1 << 26, round_size
     d_frames = torch.empty(n_fetch, dtype=torch.int32, device="cuda")
     out = {"fetches": n_fetch, "round_size": round_size, "trace_gen_s": gen_s, "unit": "fetches/s",
            "l2": "flushed before every round"}
-    runs = [("single_clock", pbm.BM_SINGLE_CLOCK, 1, 0), ("dist_clock", pbm.BM_DIST_CLOCK, 4096, 0),
-            ("single_clock_copy4k", pbm.BM_SINGLE_CLOCK, 1, 4096)]
+    # by_page: pins released by page (pbm_bufmgr_round_pages, release list
+    # naming the held-page array the rounds write), else by frame
+    runs = [("single_clock", pbm.BM_SINGLE_CLOCK, 1, 0, False), ("dist_clock", pbm.BM_DIST_CLOCK, 4096, 0, False),
+            ("single_clock_by_page", pbm.BM_SINGLE_CLOCK, 1, 0, True),
+            ("dist_clock_by_page", pbm.BM_DIST_CLOCK, 4096, 0, True),
+            ("single_clock_copy4k", pbm.BM_SINGLE_CLOCK, 1, 4096, False)]
     backing = None
-    for name, policy, arms, fsz in runs:
+    d_held = torch.empty(n_fetch, dtype=torch.int32, device="cuda")
+    for name, policy, arms, fsz, by_page in runs:
         if fsz and backing is None:
             backing = torch.empty(n_logical * fsz // 4, dtype=torch.int32, device="cuda")
         bm = pbm.BufferManager(n_logical, n_frames, frame_size=fsz, policy=policy, n_arms=arms,
                                backing=backing if fsz else None)
         d_frames.fill_(-1)
+        d_held.fill_(-1)
         t_ms = 0.0
         for r in range(rounds):
             a, b = int(ptr[r]), int(ptr[r + 1])
+            lo = r * round_size
+            rel = d_idx[a:] if b > a else None
+            if by_page:
+                fn = lambda: bm.round_pages(d_held, rel, b - a, d_pages[lo:], round_size, lo, d_frames[lo:],
+                                            d_held[lo:], stream=sh)
+            else:
+                fn = lambda: bm.round(d_frames, rel, b - a, d_pages[lo:], round_size, lo, d_frames[lo:], stream=sh)
             flush.zero_()
-            t_ms += _ev_ms(torch, stream, lambda: bm.round(d_frames, d_idx[a:] if b > a else None, b - a,
-                                                           d_pages[r * round_size:], round_size, r * round_size,
-                                                           d_frames[r * round_size:], stream=sh))
+            t_ms += _ev_ms(torch, stream, fn)
         c = bm.counters(sh)
         chk = bm.check(sh)
         out[name] = {"value": n_fetch / (t_ms * 1e-3), "ms_total": t_ms, "hits": c.hits, "misses": c.misses,
                      "evictions": c.evictions, "failures": c.failures, "hit_rate": c.hits / max(1, n_fetch),
                      "table_mismatches": chk.mismatches, "half_loaded": chk.loading,
-                     "frame_bytes": fsz, "arms": arms}
+                     "frame_bytes": fsz, "arms": arms, "release": "by page" if by_page else "by frame",
+                     "bad_unpins": c.bad_unpins, "timeouts": c.timeouts}
         bm.close()
-    del backing
+    del backing, d_held
     return out
 
 
@@ -1049,19 +1061,24 @@ def run_profile_kernel(args):
     flush = torch.empty(512 << 20, dtype=torch.uint8, device="cuda")
     out = {"profile_kernel": args.profile_kernel}
     if args.profile_kernel == "bufmgr":
-        R, rounds = 1 << 18, 16
+        R, rounds = 1 << 18, args.bm_rounds
         pages = workloads.zipf_pages(1 << 24, 0.99, R * rounds, 3)
         ptr, idx = workloads.release_lists(rounds, R, 0.25, 3)
         d_pages = torch.from_numpy(pages).cuda()
         d_idx = torch.from_numpy(idx).cuda()
         d_frames = torch.full((R * rounds,), -1, dtype=torch.int32, device="cuda")
-        bm = pbm.BufferManager(1 << 24, 1 << 20, policy=pbm.BM_SINGLE_CLOCK)
+        bm = pbm.BufferManager(1 << 24, 1 << args.bm_frames_log2, policy=pbm.BM_SINGLE_CLOCK)
+        d_held = torch.full((R * rounds,), -1, dtype=torch.int32, device="cuda")
         per_round = []
         for r in range(rounds):
             a, b = int(ptr[r]), int(ptr[r + 1])
             flush.zero_()
-            bm.round(d_frames, d_idx[a:] if b > a else None, b - a, d_pages[r * R:], R, r * R, d_frames[r * R:],
-                     stream=sh)
+            rel = d_idx[a:] if b > a else None
+            if args.bm_by_page:
+                bm.round_pages(d_held, rel, b - a, d_pages[r * R:], R, r * R, d_frames[r * R:], d_held[r * R:],
+                               stream=sh)
+            else:
+                bm.round(d_frames, rel, b - a, d_pages[r * R:], R, r * R, d_frames[r * R:], stream=sh)
             c = bm.counters(sh)
             per_round.append((c.hits, c.misses, c.evictions))
         torch.cuda.synchronize()
@@ -1305,6 +1322,12 @@ def main():
                     help="auto: the autotuner picks (untimed, before the timed steps); else a fixed walk")
     ap.add_argument("--profile-kernel", default=None, choices=["bufmgr", "malloc", "alloc", "misc", "catalog"],
                     help="a small case of another kernel, for ncu (alloc also runs the free kernel)")
+    ap.add_argument("--bm-frames-log2", type=int, default=20,
+                    help="--profile-kernel bufmgr: log2 of the frames (22 is the benchmark's buffer manager)")
+    ap.add_argument("--bm-rounds", type=int, default=16,
+                    help="--profile-kernel bufmgr: rounds of 2^18 fetches")
+    ap.add_argument("--bm-by-page", action="store_true",
+                    help="--profile-kernel bufmgr: release pins by page (pbm_bufmgr_round_pages)")
     ap.add_argument("--configs", default="all",
                     help="other workloads measured after the headline: all, none, or a comma list of "
                          "claim_write_free_50pct,occupancy_sweep,strategies,clock_churn_reference_pool,"

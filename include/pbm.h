@@ -366,18 +366,35 @@ int pbm_bufmgr_reset(pbm_bufmgr *m, void *stream);
 /* One round: unpin d_frames_of[d_release_idx[j]] for j < n_release, then
  * fetch d_pages[0..n) into d_frames_out (-1 = no frame).  Request i of the
  * round uses distributed-clock arm (slot0 + i) % n_arms.  serial != 0: one
- * thread, releases then fetches in order (deterministic replay). */
+ * thread, releases then fetches in order (deterministic replay).  In the
+ * parallel form a round's releases may land after other fetches of the same
+ * round (a sweep passes a page whose release has not landed as pinned).  A
+ * page holds at most 2^30 - 1 pins at a time.  A release of a pin that is not
+ * held is counted bad and undone; until it is undone, a fetch of the same
+ * page may see it as pinned or, if the page is not resident, wait for it.
+ * The lanes of a warp that release the same frame (or page) merge into one
+ * release, which is rejected whole if it asks for more pins than are held. */
 int pbm_bufmgr_round(pbm_bufmgr *m, const int32_t *d_frames_of, const int32_t *d_release_idx,
                      uint32_t n_release, const int32_t *d_pages, uint32_t n, uint32_t slot0,
                      int32_t *d_frames_out, int serial, void *stream);
+/* The same round with pins released by page, as a buffer pool's
+ * unpin(page) names them: unpin page d_pages_of[d_release_idx[j]] for
+ * j < n_release (negative entries are skipped), then fetch d_pages[0..n) into
+ * d_frames_out.  A release then needs no frame-to-page lookup.  d_held_out
+ * (may be NULL) receives, for each fetch, its page if it pinned a frame and
+ * -1 if it did not: an array that later rounds' release lists can name, so
+ * that no release names a fetch that holds nothing. */
+int pbm_bufmgr_round_pages(pbm_bufmgr *m, const int32_t *d_pages_of, const int32_t *d_release_idx,
+                           uint32_t n_release, const int32_t *d_pages, uint32_t n, uint32_t slot0,
+                           int32_t *d_frames_out, int32_t *d_held_out, int serial, void *stream);
 int pbm_bufmgr_stats(pbm_bufmgr *m, pbm_bufmgr_counters *h_out, void *stream);
 int pbm_bufmgr_check(pbm_bufmgr *m, pbm_bufmgr_check_result *h_out, void *stream);
 int pbm_bufmgr_frames(pbm_bufmgr *m, void **d_frames, size_t *bytes);
 /* Copies the maps to the host (either pointer may be NULL; synchronises
  * `stream`): h_page_entries[n_logical], one 64-bit word per logical page --
  * the frame holding it in the high 32 bits (signed: -1 not resident, -2 and
- * -3 a load in progress), the CLOCK reference bit in bit 31, its pins in
- * bits 0..30; h_frame_pages[n_frames], the page each frame holds
+ * -3 a load in progress), the CLOCK reference bit in bit 31, a guard bit
+ * (bit 30, set while no release is being undone), its pins in bits 0..29; h_frame_pages[n_frames], the page each frame holds
  * (0xffffffff empty).  No reference counterpart. */
 int pbm_bufmgr_read_tables(pbm_bufmgr *m, uint64_t *h_page_entries, uint32_t *h_frame_pages, void *stream);
 /* Copies the first bytes_per_frame bytes of each listed frame into d_out

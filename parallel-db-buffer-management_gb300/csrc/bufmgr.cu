@@ -9,7 +9,12 @@
 //   pt[p]          one 64-bit word per logical page: the frame holding p in
 //                  the high 32 bits (-1 not resident, -2 being loaded, -3 a
 //                  load that failed and is being left), the CLOCK reference
-//                  bit in bit 31 and the page's pins in bits 0..30
+//                  bit in bit 31, a guard bit (bit 30, always set between
+//                  operations) and the page's pins in bits 0..29.  The guard
+//                  lets a release subtract its pins first and check after:
+//                  a release of more pins than the page holds borrows from
+//                  the guard instead of the reference bit or the frame, and
+//                  is added back
 //   frame_page[f]  the page frame f holds (0xffffffff: empty)
 //   hands          SINGLE: one shared hand (atomicAdd); DIST: per-slot hands,
 //                  each starting at its own frame and advancing privately
@@ -44,14 +49,17 @@ constexpr int32_t kLoading = -2;
 constexpr int32_t kFailed = -3;
 constexpr unsigned long long kFrameUnit = 1ull << 32;
 constexpr unsigned long long kRef = 1ull << 31;
-constexpr uint32_t kPinMask = 0x7fffffffu;
-constexpr unsigned long long kEntryNotResident = (unsigned long long)(uint32_t)kNotResident << 32;
-constexpr unsigned long long kEntryFailed = (unsigned long long)(uint32_t)kFailed << 32;
+constexpr uint32_t kGuard = 1u << 30;
+constexpr uint32_t kPinField = 0x7fffffffu;   // guard + pins
+constexpr unsigned long long kEntryNotResident = ((unsigned long long)(uint32_t)kNotResident << 32) | kGuard;
+constexpr unsigned long long kEntryFailed = ((unsigned long long)(uint32_t)kFailed << 32) | kGuard;
 constexpr uint32_t kFetchSpinLimit = 1u << 16;   // polls of a page another request is loading
 constexpr uint32_t kFetchAttempts = 1024u;        // fetches retried after a failed load
 
 __device__ __forceinline__ int32_t e_frame(unsigned long long e) { return (int32_t)(e >> 32); }
-__device__ __forceinline__ uint32_t e_pins(unsigned long long e) { return (uint32_t)e & kPinMask; }
+// Pins of an entry; while another release's over-subtraction has borrowed
+// the guard, this reads as a huge count (the page counts as pinned).
+__device__ __forceinline__ uint32_t e_pins(unsigned long long e) { return ((uint32_t)e & kPinField) - kGuard; }
 __device__ __forceinline__ bool e_ref(unsigned long long e) { return (e & kRef) != 0ull; }
 
 struct BmStats {
@@ -194,7 +202,11 @@ __device__ __forceinline__ void publish(const BmView& b, uint32_t page, int32_t 
                                         BmAcc& acc) {
     if (h >= 0) {
         if (old_page != kEmptyPage) ++acc.evictions;
-        __threadfence();   // frame_page and the frame's bytes before the entry
+        // the frame's bytes before the entry that names the frame.  Without a
+        // copy nothing needs the order: a sweep that reads frame_page[h]
+        // before the entry is published, or the old page's entry after the
+        // eviction, finds an entry that does not name h and passes the frame
+        if (b.frames && b.backing) __threadfence();
         atomicAdd(b.pt + page, (unsigned long long)(h - kLoading) * kFrameUnit + kRef);
         acc.misses += 1u;
         acc.hits += k - 1u;
@@ -207,10 +219,11 @@ __device__ __forceinline__ void publish(const BmView& b, uint32_t page, int32_t 
 
 enum : int { kStHit = 1, kStLoad = 2, kStWait = 3 };
 
-// The first step of a fetch of `page` for k requests: add their pins.
-// Returns the state and, for a hit, the frame.
-__device__ __forceinline__ int begin_fetch(const BmView& b, uint32_t page, uint32_t k, int32_t* frame) {
-    const unsigned long long old = atomicAdd(b.pt + page, (unsigned long long)k);
+// The state of a fetch whose k pins were just added (`old`: the entry before
+// the add): a hit (reference bit set if it was clear), the load of
+// a page not resident and unpinned (entry marked loading), or a wait for
+// another request's load.
+__device__ __forceinline__ int fetch_state(const BmView& b, uint32_t page, unsigned long long old, int32_t* frame) {
     const int32_t f = e_frame(old);
     if (f >= 0) {
         if (!e_ref(old)) atomicOr(b.pt + page, kRef);
@@ -222,6 +235,12 @@ __device__ __forceinline__ int begin_fetch(const BmView& b, uint32_t page, uint3
         return kStLoad;
     }
     return kStWait;
+}
+
+// The first step of a fetch of `page` for k requests: add their pins.
+// Returns the state and, for a hit, the frame.
+__device__ __forceinline__ int begin_fetch(const BmView& b, uint32_t page, uint32_t k, int32_t* frame) {
+    return fetch_state(b, page, atomicAdd(b.pt + page, (unsigned long long)k), frame);
 }
 
 // A request whose pins are registered on a page another request is loading:
@@ -340,111 +359,211 @@ __device__ __forceinline__ void finish_loads_warp(const BmView& b, bool loader, 
     if (loader) publish(b, page, h, old_page, k, acc);
 }
 
-// Releases k pins of frame f (through the page it holds) with one atomic.
-// A release of more pins than the page holds (a caller error) is taken back
-// and counted as bad.
-__device__ __forceinline__ void unpin_k(const BmView& b, int32_t f, uint32_t k, unsigned long long& ok,
-                                        unsigned long long& bad) {
-    if (f < 0 || (uint32_t)f >= b.n_frames || k == 0u) return;
-    const uint32_t q = __ldcg(b.frame_page + f);
-    if (q >= b.n_logical) { bad += k; return; }
-    const unsigned long long e = __ldcg(b.pt + q);
-    if (e_frame(e) != f || e_pins(e) < k) { bad += k; return; }
-    const unsigned long long old = atomicAdd(b.pt + q, 0ull - (unsigned long long)k);
-    if (e_frame(old) != f || e_pins(old) < k) {
-        atomicAdd(b.pt + q, (unsigned long long)k);
+// A release of k pins of `page` is one atomic: subtract first, then check
+// that the page was resident -- in frame `frame` when the caller named the
+// frame (frame < 0: any frame) -- and held at least k pins.  A release that
+// was not is added back and counted bad; the guard bit keeps the borrowed
+// pins away from the reference bit and the frame meanwhile.
+__device__ __forceinline__ unsigned long long release_issue(const BmView& b, uint32_t page, uint32_t k) {
+    return atomicAdd(b.pt + page, 0ull - (unsigned long long)k);
+}
+
+__device__ __forceinline__ void release_check(const BmView& b, uint32_t page, int32_t frame, uint32_t k,
+                                              unsigned long long old, unsigned long long& ok,
+                                              unsigned long long& bad) {
+    const int32_t of = e_frame(old);
+    if (of < 0 || (frame >= 0 && of != frame) || e_pins(old) < k) {
+        atomicAdd(b.pt + page, (unsigned long long)k);
         bad += k;
         return;
     }
     ok += k;
 }
 
+// The page a release names: BYPAGE, the page itself (negative: nothing to
+// release); else a frame, whose page frame_page names.  Returns false when
+// there is nothing to release; out-of-range names are counted bad.
+template <bool BYPAGE>
+__device__ __forceinline__ bool release_target(const BmView& b, int32_t v, uint32_t k, uint32_t* page,
+                                               int32_t* frame, unsigned long long& bad) {
+    if (v < 0) return false;
+    if constexpr (BYPAGE) {
+        if ((uint32_t)v >= b.n_logical) { bad += k; return false; }
+        *page = (uint32_t)v;
+        *frame = -1;
+    } else {
+        if ((uint32_t)v >= b.n_frames) return false;
+        const uint32_t q = __ldcg(b.frame_page + v);
+        if (q >= b.n_logical) { bad += k; return false; }
+        *page = q;
+        *frame = v;
+    }
+    return true;
+}
+
+// Per-block merge tables (shared memory): the block's requests for one key
+// (a page to fetch, or a page / frame to release) meet in one slot, and the
+// first lane to claim the slot issues one atomic for all of them.  Under a
+// skewed stream the hottest pages are in nearly every warp's requests, so
+// merging within the block rather than the warp divides the atomics that
+// queue on one page's entry by the block's warps.
+constexpr uint32_t kMergeSlots = 512;            // >= 2 x the block's lanes
+constexpr uint32_t kMergeEmpty = 0xffffffffu;   // no page or frame id reaches it
+constexpr uint32_t kMergeFirst = 1u << 31;
+
+struct MergeTables {
+    uint32_t fkey[kMergeSlots];
+    uint32_t fcnt[kMergeSlots];
+    int32_t fres[kMergeSlots];
+    uint32_t rkey[kMergeSlots];
+    uint32_t rcnt[kMergeSlots];
+};
+
+// Adds c requests for `key` to a table; returns the slot, with kMergeFirst
+// set for the lane that claimed it.  A table never holds more keys than the
+// block has lanes, so a free slot is always found.
+__device__ __forceinline__ uint32_t merge_insert(uint32_t* keys, uint32_t* cnt, uint32_t key, uint32_t c) {
+    uint32_t h = (key * 2654435761u) >> 23;   // 9 bits: kMergeSlots
+    for (uint32_t probe = 0; probe < kMergeSlots; ++probe) {
+        const uint32_t prev = atomicCAS(keys + h, kMergeEmpty, key);
+        if (prev == kMergeEmpty || prev == key) {
+            atomicAdd(cnt + h, c);
+            return prev == kMergeEmpty ? (h | kMergeFirst) : h;
+        }
+        h = (h + 1u) & (kMergeSlots - 1u);
+    }
+    return kMergeEmpty;   // not reached
+}
+
+// The many-thread round.  Per block iteration every lane takes release i
+// and fetch i (i = the block's base + threadIdx.x); lanes merge by key in the
+// warp (match) and then in the block (the tables), and each key's first
+// lane issues its atomic: the fetch's pin, and the release while the pin is
+// in flight.  The fetch's result goes back through the table to every lane
+// that asked for the page.  Releases of one round may land after other
+// blocks' fetches of the same round; a sweep that meets a page whose
+// release has not landed yet passes it as pinned, as it would any pinned
+// page.
+template <bool DIST, bool BYPAGE>
+__device__ __forceinline__ void round_blocks(const BmView& b, const int32_t* release_of, const int32_t* release_idx,
+                                             uint32_t n_release, const int32_t* pages, uint32_t n, uint32_t slot0,
+                                             int32_t* frames_out, int32_t* held_out, unsigned long long& ok,
+                                             unsigned long long& bad, BmAcc& acc) {
+    __shared__ MergeTables t;
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint64_t work = n > n_release ? n : n_release;
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    // block-uniform trip count
+    for (uint64_t bbase = (uint64_t)blockIdx.x * blockDim.x; bbase < work; bbase += stride) {
+        const uint64_t i = bbase + threadIdx.x;
+        for (uint32_t s = threadIdx.x; s < kMergeSlots; s += blockDim.x) {
+            t.fkey[s] = kMergeEmpty;
+            t.fcnt[s] = 0u;
+            t.rkey[s] = kMergeEmpty;
+            t.rcnt[s] = 0u;
+        }
+        const int32_t ri = i < n_release ? __ldg(release_idx + i) : -1;
+        const int32_t p = i < n ? __ldg(pages + i) : -1;
+        const bool valid = p >= 0 && (uint32_t)p < b.n_logical;
+        const uint32_t peers = __match_any_sync(0xffffffffu, valid ? (uint32_t)p : 0x80000000u + lane);
+        const uint32_t leader = (uint32_t)__ffs((int)peers) - 1u;
+        const int32_t rv = ri >= 0 ? __ldcg(release_of + ri) : -1;
+        const uint32_t rpeers = __match_any_sync(0xffffffffu, rv >= 0 ? (uint32_t)rv : 0x80000000u + lane);
+        __syncthreads();   // tables clear
+        uint32_t fslot = kMergeEmpty, rslot = kMergeEmpty;
+        if (valid && lane == leader) fslot = merge_insert(t.fkey, t.fcnt, (uint32_t)p, (uint32_t)__popc(peers));
+        if (rv >= 0 && (uint32_t)(__ffs((int)rpeers) - 1) == lane)
+            rslot = merge_insert(t.rkey, t.rcnt, (uint32_t)rv, (uint32_t)__popc(rpeers));
+        __syncthreads();   // counts complete
+        // the key's first lane: one atomic for all the block's requests
+        const bool lead = fslot != kMergeEmpty && (fslot & kMergeFirst);
+        const uint32_t k = lead ? t.fcnt[fslot & ~kMergeFirst] : 0u;
+        unsigned long long fold = 0;
+        if (lead) fold = atomicAdd(b.pt + p, (unsigned long long)k);
+        uint32_t rq = 0;
+        int32_t rf = -1;
+        const bool rlead = rslot != kMergeEmpty && (rslot & kMergeFirst) &&
+                           release_target<BYPAGE>(b, rv, t.rcnt[rslot & ~kMergeFirst], &rq, &rf, bad);
+        const uint32_t rk = rlead ? t.rcnt[rslot & ~kMergeFirst] : 0u;
+        unsigned long long rold = 0;
+        if (rlead) rold = release_issue(b, rq, rk);
+        const uint32_t slot = (slot0 + (uint32_t)i) % b.n_arms;
+        int32_t f = -1;
+        int st = 0;
+        if (lead) st = fetch_state(b, (uint32_t)p, fold, &f);
+        if (rlead) release_check(b, rq, rf, rk, rold, ok, bad);
+        if (st == kStHit) acc.hits += k;
+        if constexpr (!DIST) {
+            // the single hand's loaders of the warp sweep together
+            const uint32_t lm = __ballot_sync(0xffffffffu, st == kStLoad);
+            if (lm) {
+                uint32_t old_page = kEmptyPage;
+                const int32_t h = sweep_warp(b, lm, (uint32_t)p, &old_page);
+                finish_loads_warp(b, st == kStLoad, (uint32_t)p, h, old_page, k, acc);
+                if (st == kStLoad) f = h;
+            }
+        } else if (st == kStLoad) {
+            uint32_t old_page = kEmptyPage;
+            const int32_t h = sweep_private(b, (uint32_t)p, slot, &old_page);
+            if (h >= 0 && b.backing && b.frames) copy_frame(b, (uint32_t)p, h);
+            publish(b, (uint32_t)p, h, old_page, k, acc);
+            f = h;
+        }
+        if (st == kStWait) {
+            f = wait_loaded(b, (uint32_t)p);
+            if (f >= 0) {
+                acc.hits += k;
+            } else {
+                leave(b, (uint32_t)p, k);
+                if (f == kLoading) {
+                    acc.timeouts += k;
+                    f = -1;
+                } else {
+                    f = fetch_k<DIST>(b, (uint32_t)p, slot, k, acc);   // the load failed: try once more
+                }
+            }
+        }
+        if (lead) t.fres[fslot & ~kMergeFirst] = f;
+        __syncthreads();   // results in the table
+        const uint32_t my_slot = __shfl_sync(0xffffffffu, fslot, (int)leader) & ~kMergeFirst;
+        if (i < n) {
+            const int32_t got = valid ? t.fres[my_slot] : -1;
+            frames_out[i] = got;
+            if (held_out) held_out[i] = got >= 0 ? p : -1;
+        }
+        __syncthreads();   // the tables are reused by the next iteration
+    }
+}
+
 // One round: release the listed pins, then fetch this round's pages.
 // With one thread this is the deterministic replay of the round.
-// DIST: per-slot hands (b.dist), else the single shared hand.
-template <bool DIST>
-__global__ void __launch_bounds__(256) k_round(BmView b, const int32_t* release_frames_of,
-                                               const int32_t* release_idx, uint32_t n_release,
-                                               const int32_t* pages, uint32_t n, uint32_t slot0,
-                                               int32_t* frames_out) {
-    const uint64_t tid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    const uint64_t nthr = (uint64_t)gridDim.x * blockDim.x;
+// DIST: per-slot hands (b.dist), else the single shared hand.  BYPAGE:
+// release_of names pages, else frames.  held_out (may be null) receives
+// each fetch's page, or -1 where the fetch got no frame.
+template <bool DIST, bool BYPAGE>
+__global__ void __launch_bounds__(256) k_round(BmView b, const int32_t* release_of, const int32_t* release_idx,
+                                               uint32_t n_release, const int32_t* pages, uint32_t n, uint32_t slot0,
+                                               int32_t* frames_out, int32_t* held_out) {
     unsigned long long ok = 0, bad = 0;
-    if (nthr == 1u) {
-        for (uint32_t j = 0; j < n_release; ++j) unpin_k(b, release_frames_of[release_idx[j]], 1u, ok, bad);
-    } else {
-        // warp-uniform trip count: lanes releasing pins of the same frame (hot
-        // pages of a skewed stream) merge them into one atomic
-        const uint32_t lane = threadIdx.x & 31u;
-        for (uint64_t base = tid - lane; base < n_release; base += nthr) {
-            const uint64_t j = base + lane;
-            const int32_t f = j < n_release ? release_frames_of[release_idx[j]] : -1;
-            const bool valid = f >= 0 && (uint32_t)f < b.n_frames;
-            const uint32_t peers = __match_any_sync(0xffffffffu, valid ? (uint32_t)f : 0x80000000u + lane);
-            if (valid && (uint32_t)(__ffs((int)peers) - 1) == lane) unpin_k(b, f, (uint32_t)__popc(peers), ok, bad);
-        }
-    }
     BmAcc acc;
-    if (nthr == 1u) {
+    if ((uint64_t)gridDim.x * blockDim.x == 1u) {
+        for (uint32_t j = 0; j < n_release; ++j) {
+            uint32_t q;
+            int32_t fr;
+            if (release_target<BYPAGE>(b, release_of[release_idx[j]], 1u, &q, &fr, bad))
+                release_check(b, q, fr, 1u, release_issue(b, q, 1u), ok, bad);
+        }
         __threadfence();
         for (uint32_t i = 0; i < n; ++i) {
             int32_t p = pages[i];
             int32_t f = -1;
             if (p >= 0 && (uint32_t)p < b.n_logical) f = fetch_k<DIST>(b, (uint32_t)p, (slot0 + i) % b.n_arms, 1u, acc);
             frames_out[i] = f;
+            if (held_out) held_out[i] = f >= 0 ? p : -1;
         }
     } else {
-        // warp-uniform trip count (blockDim is a multiple of 32); the lanes
-        // fetching one page merge into their leader, whose atomic pins the
-        // page for all of them
-        const uint32_t lane = threadIdx.x & 31u;
-        for (uint64_t base = tid - lane; base < n; base += nthr) {
-            const uint64_t i = base + lane;
-            const int32_t p = i < n ? pages[i] : -1;
-            const bool valid = p >= 0 && (uint32_t)p < b.n_logical;
-            const uint32_t key = valid ? (uint32_t)p : 0x80000000u + lane;   // invalid lanes never merge
-            const uint32_t peers = __match_any_sync(0xffffffffu, key);
-            const uint32_t leader = (uint32_t)__ffs((int)peers) - 1u;
-            const uint32_t k = (uint32_t)__popc(peers);
-            const bool lead = valid && lane == leader;
-            const uint32_t slot = (slot0 + (uint32_t)i) % b.n_arms;
-            int32_t f = -1;
-            int st = 0;
-            if (lead) st = begin_fetch(b, (uint32_t)p, k, &f);
-            if (st == kStHit) acc.hits += k;
-            if constexpr (!DIST) {
-                // the single hand's loaders sweep together
-                const uint32_t lm = __ballot_sync(0xffffffffu, st == kStLoad);
-                if (lm) {
-                    uint32_t old_page = kEmptyPage;
-                    const int32_t h = sweep_warp(b, lm, (uint32_t)p, &old_page);
-                    finish_loads_warp(b, st == kStLoad, (uint32_t)p, h, old_page, k, acc);
-                    if (st == kStLoad) f = h;
-                }
-            } else if (st == kStLoad) {
-                uint32_t old_page = kEmptyPage;
-                const int32_t h = sweep_private(b, (uint32_t)p, slot, &old_page);
-                if (h >= 0 && b.backing && b.frames) copy_frame(b, (uint32_t)p, h);
-                publish(b, (uint32_t)p, h, old_page, k, acc);
-                f = h;
-            }
-            if (st == kStWait) {
-                f = wait_loaded(b, (uint32_t)p);
-                if (f >= 0) {
-                    acc.hits += k;
-                } else {
-                    leave(b, (uint32_t)p, k);
-                    if (f == kLoading) {
-                        acc.timeouts += k;
-                        f = -1;
-                    } else {
-                        f = fetch_k<DIST>(b, (uint32_t)p, slot, k, acc);   // the load failed: try once more
-                    }
-                }
-            }
-            f = __shfl_sync(0xffffffffu, f, (int)leader);
-            if (i < n) frames_out[i] = valid ? f : -1;
-        }
+        round_blocks<DIST, BYPAGE>(b, release_of, release_idx, n_release, pages, n, slot0, frames_out, held_out, ok,
+                                   bad, acc);
     }
     block_add_counters<7>({ok, bad, acc.hits, acc.misses, acc.evictions, acc.failures, acc.timeouts},
                           {&b.stats->unpins, &b.stats->bad_unpins, &b.stats->hits, &b.stats->misses,
@@ -586,24 +705,49 @@ int pbm_bufmgr_reset(pbm_bufmgr* m, void* stream) {
     return PBM_OK;
 }
 
-int pbm_bufmgr_round(pbm_bufmgr* m, const int32_t* d_frames_of, const int32_t* d_release_idx,
-                     uint32_t n_release, const int32_t* d_pages, uint32_t n, uint32_t slot0,
-                     int32_t* d_frames_out, int serial, void* stream) {
-    if (!m || (n_release && (!d_frames_of || !d_release_idx)) || (n && (!d_pages || !d_frames_out)))
+}  // extern "C"
+
+namespace {
+
+int launch_round(pbm_bufmgr* m, bool by_page, const int32_t* d_release_of, const int32_t* d_release_idx,
+                 uint32_t n_release, const int32_t* d_pages, uint32_t n, uint32_t slot0, int32_t* d_frames_out,
+                 int32_t* d_held_out, int serial, void* stream) {
+    if (!m || (n_release && (!d_release_of || !d_release_idx)) || (n && (!d_pages || !d_frames_out)))
         return PBM_ERR_INVALID;
     pbm::DeviceScope scope(m->device);
     if (n == 0 && n_release == 0) return PBM_OK;
     const uint32_t work = n > n_release ? n : n_release;
-    int block = serial ? 1 : 256;
-    int grid = serial ? 1 : (int)((work + 255u) / 256u);
+    const int block = serial ? 1 : 256;
+    const int grid = serial ? 1 : (int)((work + 255u) / 256u);
+    cudaStream_t s = (cudaStream_t)stream;
+    auto go = [&](auto kernel) {
+        kernel<<<grid, block, 0, s>>>(m->v, d_release_of, d_release_idx, n_release, d_pages, n, slot0, d_frames_out,
+                                      d_held_out);
+    };
     if (m->v.dist)
-        k_round<true><<<grid, block, 0, (cudaStream_t)stream>>>(m->v, d_frames_of, d_release_idx, n_release,
-                                                                d_pages, n, slot0, d_frames_out);
+        by_page ? go(k_round<true, true>) : go(k_round<true, false>);
     else
-        k_round<false><<<grid, block, 0, (cudaStream_t)stream>>>(m->v, d_frames_of, d_release_idx, n_release,
-                                                                 d_pages, n, slot0, d_frames_out);
+        by_page ? go(k_round<false, true>) : go(k_round<false, false>);
     PBM_LAUNCH_CHECK();
     return PBM_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int pbm_bufmgr_round(pbm_bufmgr* m, const int32_t* d_frames_of, const int32_t* d_release_idx,
+                     uint32_t n_release, const int32_t* d_pages, uint32_t n, uint32_t slot0,
+                     int32_t* d_frames_out, int serial, void* stream) {
+    return launch_round(m, false, d_frames_of, d_release_idx, n_release, d_pages, n, slot0, d_frames_out, nullptr,
+                        serial, stream);
+}
+
+int pbm_bufmgr_round_pages(pbm_bufmgr* m, const int32_t* d_pages_of, const int32_t* d_release_idx,
+                           uint32_t n_release, const int32_t* d_pages, uint32_t n, uint32_t slot0,
+                           int32_t* d_frames_out, int32_t* d_held_out, int serial, void* stream) {
+    return launch_round(m, true, d_pages_of, d_release_idx, n_release, d_pages, n, slot0, d_frames_out, d_held_out,
+                        serial, stream);
 }
 
 int pbm_bufmgr_stats(pbm_bufmgr* m, pbm_bufmgr_counters* h_out, void* stream) {

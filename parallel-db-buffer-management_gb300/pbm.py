@@ -202,6 +202,8 @@ SIGNATURES = [
     ("pbm_bufmgr_reset", c_int, [c_void_p, c_void_p]),
     ("pbm_bufmgr_round", c_int, [c_void_p, c_void_p, c_void_p, c_uint32, c_void_p, c_uint32, c_uint32,
                                  c_void_p, c_int, c_void_p]),
+    ("pbm_bufmgr_round_pages", c_int, [c_void_p, c_void_p, c_void_p, c_uint32, c_void_p, c_uint32, c_uint32,
+                                       c_void_p, c_void_p, c_int, c_void_p]),
     ("pbm_bufmgr_stats", c_int, [c_void_p, POINTER(BufMgrCounters), c_void_p]),
     ("pbm_bufmgr_check", c_int, [c_void_p, POINTER(BufMgrCheck), c_void_p]),
     ("pbm_bufmgr_frames", c_int, [c_void_p, POINTER(c_void_p), POINTER(c_size_t)]),
@@ -507,6 +509,15 @@ class BufferManager:
                       self.lib.pbm_bufmgr_round(self.h, _ptr(frames_of), _ptr(release_idx), n_release,
                                                 _ptr(pages), n, slot0, _ptr(frames_out), int(serial), stream))
 
+    def round_pages(self, pages_of, release_idx, n_release, pages, n, slot0, frames_out, held_out=None,
+                    serial=False, stream=0):
+        """The round with pins released by page (pages_of[release_idx[j]]);
+        held_out, if given, receives each fetch's page (-1: no frame)."""
+        return _check("pbm_bufmgr_round_pages",
+                      self.lib.pbm_bufmgr_round_pages(self.h, _ptr(pages_of), _ptr(release_idx), n_release,
+                                                      _ptr(pages), n, slot0, _ptr(frames_out), _ptr(held_out),
+                                                      int(serial), stream))
+
     def reset(self, stream=0):
         _check("pbm_bufmgr_reset", self.lib.pbm_bufmgr_reset(self.h, stream))
 
@@ -534,7 +545,7 @@ class BufferManager:
         _check("pbm_bufmgr_read_tables",
                self.lib.pbm_bufmgr_read_tables(self.h, e.ctypes.data, fp.ctypes.data, stream))
         frame = (e >> np.uint64(32)).astype(np.uint32).view(np.int32)
-        pins = (e & np.uint64(0x7fffffff)).astype(np.int64)
+        pins = (e & np.uint64(0x3fffffff)).astype(np.int64)
         ref = ((e >> np.uint64(31)) & np.uint64(1)).astype(bool)
         return frame, pins, ref, fp.view(np.int32)
 

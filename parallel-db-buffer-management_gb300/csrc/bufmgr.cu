@@ -105,19 +105,24 @@ __device__ __forceinline__ bool take_frame(const BmView& b, uint32_t f, uint32_t
 
 // One frame under the hand: 0 pass, 1 candidate (q, e filled in).  A
 // referenced frame loses its reference bit here (second chance).
+// judge: the same for frame f holding page q whose entry e was read.
+__device__ __forceinline__ bool judge(const BmView& b, uint32_t f, uint32_t q, unsigned long long e) {
+    if (q == kEmptyPage) return true;
+    if (q >= b.n_logical) return false;
+    if (e_frame(e) != (int32_t)f || e_pins(e) != 0u) return false;   // pinned, or changing hands
+    if (e_ref(e)) {
+        atomicAnd(b.pt + q, ~kRef);
+        return false;
+    }
+    return true;
+}
+
 __device__ __forceinline__ int examine(const BmView& b, uint32_t f, uint32_t* q_out, unsigned long long* e_out) {
     const uint32_t q = __ldcg(b.frame_page + f);
     *q_out = q;
-    if (q == kEmptyPage) return 1;
-    if (q >= b.n_logical) return 0;
-    const unsigned long long e = __ldcg(b.pt + q);
+    const unsigned long long e = (q < b.n_logical) ? __ldcg(b.pt + q) : 0ull;
     *e_out = e;
-    if (e_frame(e) != (int32_t)f || e_pins(e) != 0u) return 0;   // pinned, or changing hands
-    if (e_ref(e)) {
-        atomicAnd(b.pt + q, ~kRef);
-        return 0;
-    }
-    return 1;
+    return judge(b, f, q, e) ? 1 : 0;
 }
 
 // Per-slot hand (DistClock, parallelPage.cu:571-592): the slot's hand is
@@ -291,47 +296,71 @@ __device__ __forceinline__ int32_t fetch_k(const BmView& b, uint32_t page, uint3
 
 // Warp-cooperative CLOCK sweep on the single hand.  The lanes in `loaders`
 // (each the loader of its own `page`, its entry already marked loading) need
-// victim frames.  Per batch the warp takes 32 consecutive hand positions
+// victim frames.  Per window the warp takes 32 consecutive hand positions
 // with one atomicAdd and every lane examines one frame, as the one-thread
 // sweep does.  Candidates go in hand order to the loaders in lane order,
 // each taken with the one-thread sweep's compare-and-swap (a pin that
 // arrived in between makes it fail and the loader waits for the next
-// batch); candidates beyond the loaders' need are passed.  A loader gives up
-// after its max_sweep positions.  The whole warp calls converged; returns
-// the lane's frame (-1 if none) and the page it held.
-__device__ __forceinline__ int32_t sweep_warp(const BmView& b, uint32_t loaders, uint32_t page,
-                                              uint32_t* old_page) {
+// window); candidates beyond the loaders' need are passed.  A loader gives
+// up after its max_sweep positions.  The whole warp calls converged.
+struct SweepWin {
+    uint32_t f, q;           // this lane's frame and the page it held
+    unsigned long long e;    // that page's entry as read
+    bool cand;
+};
+
+__device__ __forceinline__ SweepWin sweep_window(const BmView& b) {
+    unsigned long long base = 0;
+    if ((threadIdx.x & 31u) == 0u) base = atomicAdd(b.single_hand, 32ull);
+    base = __shfl_sync(0xffffffffu, base, 0);
+    SweepWin w;
+    w.f = (uint32_t)((base + (threadIdx.x & 31u)) % b.n_frames);
+    w.cand = examine(b, w.f, &w.q, &w.e) != 0;
+    return w;
+}
+
+// Hands one window's candidates to the loaders; returns the loaders still
+// without a frame.  *out / *old_page: the lane's frame and the page it held.
+__device__ __forceinline__ uint32_t sweep_assign(const BmView& b, const SweepWin& w, uint32_t loaders,
+                                                 uint32_t page, int32_t* out, uint32_t* old_page) {
     const uint32_t lane = threadIdx.x & 31u;
     const uint32_t lt = (1u << lane) - 1u;
+    const uint32_t cm = __ballot_sync(0xffffffffu, w.cand);
+    const int n_load = __popc(loaders);
+    // candidate of rank k serves the loader of rank k
+    const int k = __popc(cm & lt);
+    const int target = (w.cand && k < n_load) ? (int)nth_set_bit(loaders, k) : -1;
+    const uint32_t tpage = __shfl_sync(0xffffffffu, page, target < 0 ? (int)lane : target);
+    uint32_t victim_old = kEmptyPage;
+    const bool took = target >= 0 && take_frame(b, w.f, w.q, w.e, tpage, &victim_old);
+    const uint32_t tm = __ballot_sync(0xffffffffu, took);
+    const bool is_loader = (loaders >> lane) & 1u;
+    const int r = __popc(loaders & lt);
+    const int src = (is_loader && r < __popc(cm)) ? (int)nth_set_bit(cm, r) : -1;
+    const uint32_t got_f = __shfl_sync(0xffffffffu, w.f, src < 0 ? (int)lane : src);
+    const uint32_t got_old = __shfl_sync(0xffffffffu, victim_old, src < 0 ? (int)lane : src);
+    if (src >= 0 && ((tm >> src) & 1u)) {
+        *out = (int32_t)got_f;
+        *old_page = got_old;
+    }
+    return __ballot_sync(0xffffffffu, is_loader && *out < 0);
+}
+
+// The whole sweep: `first`, if given, is a window the warp already took and
+// examined (it counts against max_sweep).  Returns the lane's frame (-1 if
+// none) and the page it held.
+__device__ __forceinline__ int32_t sweep_warp(const BmView& b, uint32_t loaders, uint32_t page, uint32_t* old_page,
+                                              const SweepWin* first = nullptr) {
     int32_t out = -1;
-    const uint32_t max_batches = b.max_sweep > 32u ? (b.max_sweep + 31u) / 32u : 1u;
-    for (uint32_t it = 0; loaders != 0u && it < max_batches; ++it) {
-        unsigned long long base = 0;
-        if (lane == 0u) base = atomicAdd(b.single_hand, 32ull);
-        base = __shfl_sync(0xffffffffu, base, 0);
-        const uint32_t f = (uint32_t)((base + lane) % b.n_frames);
-        uint32_t q = kEmptyPage;
-        unsigned long long e = 0;
-        const bool cand = examine(b, f, &q, &e) != 0;
-        const uint32_t cm = __ballot_sync(0xffffffffu, cand);
-        const int n_load = __popc(loaders);
-        // candidate of rank k serves the loader of rank k
-        const int k = __popc(cm & lt);
-        const int target = (cand && k < n_load) ? (int)nth_set_bit(loaders, k) : -1;
-        const uint32_t tpage = __shfl_sync(0xffffffffu, page, target < 0 ? (int)lane : target);
-        uint32_t victim_old = kEmptyPage;
-        const bool took = target >= 0 && take_frame(b, f, q, e, tpage, &victim_old);
-        const uint32_t tm = __ballot_sync(0xffffffffu, took);
-        const bool is_loader = (loaders >> lane) & 1u;
-        const int r = __popc(loaders & lt);
-        const int src = (is_loader && r < __popc(cm)) ? (int)nth_set_bit(cm, r) : -1;
-        const uint32_t got_f = __shfl_sync(0xffffffffu, f, src < 0 ? (int)lane : src);
-        const uint32_t got_old = __shfl_sync(0xffffffffu, victim_old, src < 0 ? (int)lane : src);
-        if (src >= 0 && ((tm >> src) & 1u)) {
-            out = (int32_t)got_f;
-            *old_page = got_old;
-        }
-        loaders = __ballot_sync(0xffffffffu, is_loader && out < 0);
+    const uint32_t max_windows = b.max_sweep > 32u ? (b.max_sweep + 31u) / 32u : 1u;
+    uint32_t it = 0;
+    if (first) {
+        loaders = sweep_assign(b, *first, loaders, page, &out, old_page);
+        it = 1;
+    }
+    for (; loaders != 0u && it < max_windows; ++it) {
+        const SweepWin w = sweep_window(b);
+        loaders = sweep_assign(b, w, loaders, page, &out, old_page);
     }
     return out;
 }
@@ -402,34 +431,33 @@ __device__ __forceinline__ bool release_target(const BmView& b, int32_t v, uint3
 }
 
 // Per-block merge tables (shared memory): the block's requests for one key
-// (a page to fetch, or a page / frame to release) meet in one slot, and the
-// first lane to claim the slot issues one atomic for all of them.  Under a
+// meet in one slot, and one lane issues one atomic for all of them.  Under a
 // skewed stream the hottest pages are in nearly every warp's requests, so
 // merging within the block rather than the warp divides the atomics that
-// queue on one page's entry by the block's warps.
-constexpr uint32_t kMergeSlots = 512;            // >= 2 x the block's lanes
+// queue on one page's entry by the block's warps.  Releases by page share
+// the fetches' table: a block that releases and fetches one page moves its
+// pins with one atomic.
+constexpr uint32_t kMergeSlots = 1024;           // >= 2 x the keys of one block (256 fetches + 256 releases)
 constexpr uint32_t kMergeEmpty = 0xffffffffu;   // no page or frame id reaches it
 constexpr uint32_t kMergeFirst = 1u << 31;
 
 struct MergeTables {
-    uint32_t fkey[kMergeSlots];
-    uint32_t fcnt[kMergeSlots];
-    int32_t fres[kMergeSlots];
-    uint32_t rkey[kMergeSlots];
+    uint32_t fkey[kMergeSlots];   // pages (and, releasing by page, released pages)
+    uint32_t fcnt[kMergeSlots];   // fetches of the page
+    uint32_t frel[kMergeSlots];   // releases of the page (releasing by page)
+    int32_t fres[kMergeSlots];    // the fetch's frame
+    uint32_t rkey[kMergeSlots];   // released frames (releasing by frame)
     uint32_t rcnt[kMergeSlots];
 };
 
-// Adds c requests for `key` to a table; returns the slot, with kMergeFirst
-// set for the lane that claimed it.  A table never holds more keys than the
-// block has lanes, so a free slot is always found.
+// Adds c to cnt[slot of key]; returns the slot, with kMergeFirst set for the
+// lane whose add came first (the slot's leader for that count).  A table
+// never holds more keys than half its slots, so a slot is found.
 __device__ __forceinline__ uint32_t merge_insert(uint32_t* keys, uint32_t* cnt, uint32_t key, uint32_t c) {
-    uint32_t h = (key * 2654435761u) >> 23;   // 9 bits: kMergeSlots
+    uint32_t h = (key * 2654435761u) >> 22;   // 10 bits: kMergeSlots
     for (uint32_t probe = 0; probe < kMergeSlots; ++probe) {
         const uint32_t prev = atomicCAS(keys + h, kMergeEmpty, key);
-        if (prev == kMergeEmpty || prev == key) {
-            atomicAdd(cnt + h, c);
-            return prev == kMergeEmpty ? (h | kMergeFirst) : h;
-        }
+        if (prev == kMergeEmpty || prev == key) return atomicAdd(cnt + h, c) == 0u ? (h | kMergeFirst) : h;
         h = (h + 1u) & (kMergeSlots - 1u);
     }
     return kMergeEmpty;   // not reached
@@ -437,13 +465,17 @@ __device__ __forceinline__ uint32_t merge_insert(uint32_t* keys, uint32_t* cnt, 
 
 // The many-thread round.  Per block iteration every lane takes release i
 // and fetch i (i = the block's base + threadIdx.x); lanes merge by key in the
-// warp (match) and then in the block (the tables), and each key's first
-// lane issues its atomic: the fetch's pin, and the release while the pin is
-// in flight.  The fetch's result goes back through the table to every lane
-// that asked for the page.  Releases of one round may land after other
-// blocks' fetches of the same round; a sweep that meets a page whose
-// release has not landed yet passes it as pinned, as it would any pinned
-// page.
+// warp (match) and then in the block (the tables), and each key's leader
+// issues its atomic: the fetch's pin (with the block's releases of the page,
+// releasing by page), and other releases while the pins are in flight.  The
+// fetch's result goes back through the table to every lane that asked for
+// the page.  With the single hand each warp also takes and examines its
+// first sweep window while its pins are in flight: nearly every warp has a
+// miss, and one that has none has still moved the hand over 32 frames as a
+// sweep does (clearing reference bits, evicting nothing).  Releases of one
+// round may land after other blocks' fetches of the same round; a sweep
+// that meets a page whose release has not landed yet passes it as pinned,
+// as it would any pinned page.
 template <bool DIST, bool BYPAGE>
 __device__ __forceinline__ void round_blocks(const BmView& b, const int32_t* release_of, const int32_t* release_idx,
                                              uint32_t n_release, const int32_t* pages, uint32_t n, uint32_t slot0,
@@ -456,52 +488,86 @@ __device__ __forceinline__ void round_blocks(const BmView& b, const int32_t* rel
     // block-uniform trip count
     for (uint64_t bbase = (uint64_t)blockIdx.x * blockDim.x; bbase < work; bbase += stride) {
         const uint64_t i = bbase + threadIdx.x;
+        unsigned long long hbase = 0;
+        if (!DIST && lane == 0u) hbase = atomicAdd(b.single_hand, 32ull);   // the first sweep window
+        const int32_t ri = i < n_release ? __ldg(release_idx + i) : -1;
+        const int32_t p = i < n ? __ldg(pages + i) : -1;
         for (uint32_t s = threadIdx.x; s < kMergeSlots; s += blockDim.x) {
             t.fkey[s] = kMergeEmpty;
             t.fcnt[s] = 0u;
-            t.rkey[s] = kMergeEmpty;
-            t.rcnt[s] = 0u;
+            t.frel[s] = 0u;
+            if (!BYPAGE) {
+                t.rkey[s] = kMergeEmpty;
+                t.rcnt[s] = 0u;
+            }
         }
-        const int32_t ri = i < n_release ? __ldg(release_idx + i) : -1;
-        const int32_t p = i < n ? __ldg(pages + i) : -1;
+        SweepWin w0{};
+        if (!DIST) {
+            hbase = __shfl_sync(0xffffffffu, hbase, 0);
+            w0.f = (uint32_t)((hbase + lane) % b.n_frames);
+            w0.q = __ldcg(b.frame_page + w0.f);
+        }
         const bool valid = p >= 0 && (uint32_t)p < b.n_logical;
         const uint32_t peers = __match_any_sync(0xffffffffu, valid ? (uint32_t)p : 0x80000000u + lane);
         const uint32_t leader = (uint32_t)__ffs((int)peers) - 1u;
         const int32_t rv = ri >= 0 ? __ldcg(release_of + ri) : -1;
         const uint32_t rpeers = __match_any_sync(0xffffffffu, rv >= 0 ? (uint32_t)rv : 0x80000000u + lane);
+        // releases by page name pages outside the table's range as bad here
+        const bool rin = rv >= 0 && (!BYPAGE || (uint32_t)rv < b.n_logical);
+        if (BYPAGE && rv >= 0 && !rin && (uint32_t)(__ffs((int)rpeers) - 1) == lane) bad += (uint32_t)__popc(rpeers);
         __syncthreads();   // tables clear
         uint32_t fslot = kMergeEmpty, rslot = kMergeEmpty;
         if (valid && lane == leader) fslot = merge_insert(t.fkey, t.fcnt, (uint32_t)p, (uint32_t)__popc(peers));
-        if (rv >= 0 && (uint32_t)(__ffs((int)rpeers) - 1) == lane)
-            rslot = merge_insert(t.rkey, t.rcnt, (uint32_t)rv, (uint32_t)__popc(rpeers));
+        if (rin && (uint32_t)(__ffs((int)rpeers) - 1) == lane)
+            rslot = BYPAGE ? merge_insert(t.fkey, t.frel, (uint32_t)rv, (uint32_t)__popc(rpeers))
+                           : merge_insert(t.rkey, t.rcnt, (uint32_t)rv, (uint32_t)__popc(rpeers));
         __syncthreads();   // counts complete
-        // the key's first lane: one atomic for all the block's requests
+        if (!DIST) w0.e = w0.q < b.n_logical ? __ldcg(b.pt + w0.q) : 0ull;
+        // the page's fetch leader moves the block's pins of it with one atomic
         const bool lead = fslot != kMergeEmpty && (fslot & kMergeFirst);
-        const uint32_t k = lead ? t.fcnt[fslot & ~kMergeFirst] : 0u;
+        const uint32_t fs = fslot & ~kMergeFirst;
+        const uint32_t k = lead ? t.fcnt[fs] : 0u;
+        const uint32_t kr = (BYPAGE && lead) ? t.frel[fs] : 0u;
         unsigned long long fold = 0;
-        if (lead) fold = atomicAdd(b.pt + p, (unsigned long long)k);
-        uint32_t rq = 0;
+        if (lead) fold = atomicAdd(b.pt + p, (unsigned long long)k - (unsigned long long)kr);
+        // releases the fetches did not take along
+        const uint32_t rs = rslot & ~kMergeFirst;
+        uint32_t rq = 0, rk = 0;
         int32_t rf = -1;
-        const bool rlead = rslot != kMergeEmpty && (rslot & kMergeFirst) &&
-                           release_target<BYPAGE>(b, rv, t.rcnt[rslot & ~kMergeFirst], &rq, &rf, bad);
-        const uint32_t rk = rlead ? t.rcnt[rslot & ~kMergeFirst] : 0u;
+        bool rlead = rslot != kMergeEmpty && (rslot & kMergeFirst);
+        if (BYPAGE && rlead && t.fcnt[rs] != 0u) rlead = false;
+        if (rlead) {
+            rk = BYPAGE ? t.frel[rs] : t.rcnt[rs];
+            rlead = release_target<BYPAGE>(b, rv, rk, &rq, &rf, bad);
+        }
         unsigned long long rold = 0;
         if (rlead) rold = release_issue(b, rq, rk);
         const uint32_t slot = (slot0 + (uint32_t)i) % b.n_arms;
         int32_t f = -1;
         int st = 0;
-        if (lead) st = fetch_state(b, (uint32_t)p, fold, &f);
+        if (lead) {
+            if (kr) {
+                if (e_frame(fold) < 0 || e_pins(fold) < kr) {   // the releases held no such pins
+                    atomicAdd(b.pt + p, (unsigned long long)kr);
+                    bad += kr;
+                } else {
+                    ok += kr;
+                    fold -= kr;   // the entry after the releases, before the fetches' pins
+                }
+            }
+            st = fetch_state(b, (uint32_t)p, fold, &f);
+        }
         if (rlead) release_check(b, rq, rf, rk, rold, ok, bad);
         if (st == kStHit) acc.hits += k;
         if constexpr (!DIST) {
-            // the single hand's loaders of the warp sweep together
+            // the single hand's loaders of the warp sweep together, starting
+            // with the window taken above
+            w0.cand = judge(b, w0.f, w0.q, w0.e);
             const uint32_t lm = __ballot_sync(0xffffffffu, st == kStLoad);
-            if (lm) {
-                uint32_t old_page = kEmptyPage;
-                const int32_t h = sweep_warp(b, lm, (uint32_t)p, &old_page);
-                finish_loads_warp(b, st == kStLoad, (uint32_t)p, h, old_page, k, acc);
-                if (st == kStLoad) f = h;
-            }
+            uint32_t old_page = kEmptyPage;
+            const int32_t h = sweep_warp(b, lm, (uint32_t)p, &old_page, &w0);
+            if (lm) finish_loads_warp(b, st == kStLoad, (uint32_t)p, h, old_page, k, acc);
+            if (st == kStLoad) f = h;
         } else if (st == kStLoad) {
             uint32_t old_page = kEmptyPage;
             const int32_t h = sweep_private(b, (uint32_t)p, slot, &old_page);
@@ -523,7 +589,7 @@ __device__ __forceinline__ void round_blocks(const BmView& b, const int32_t* rel
                 }
             }
         }
-        if (lead) t.fres[fslot & ~kMergeFirst] = f;
+        if (lead) t.fres[fs] = f;
         __syncthreads();   // results in the table
         const uint32_t my_slot = __shfl_sync(0xffffffffu, fslot, (int)leader) & ~kMergeFirst;
         if (i < n) {

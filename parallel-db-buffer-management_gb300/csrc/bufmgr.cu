@@ -365,23 +365,42 @@ __device__ __forceinline__ int32_t sweep_warp(const BmView& b, uint32_t loaders,
     return out;
 }
 
-// The loaders' side of a cooperative miss: copy each new page from the
-// backing store with the whole warp (one loader at a time, 16 bytes per lane
-// per step), then publish the entries.  The whole warp calls converged.
+// The loaders' side of a cooperative miss: copy the new pages from the
+// backing store with the whole warp, then publish the entries.  The warp's
+// copies are one flat run of 16-byte pieces (loader by loader, piece by
+// piece); each lane has kCopyInFlight of its pieces loading at once before
+// it stores them, so a warp keeps 32 x kCopyInFlight loads in flight across
+// its loaders' pages.  The whole warp calls converged.
+constexpr uint32_t kCopyInFlight = 4;
+
+template <bool COPY>
 __device__ __forceinline__ void finish_loads_warp(const BmView& b, bool loader, uint32_t page, int32_t h,
                                                   uint32_t old_page, uint32_t k, BmAcc& acc) {
-    if (b.backing && b.frames) {
+    if (COPY) {
         const uint32_t lane = threadIdx.x & 31u;
         const uint32_t n16 = b.frame_size / 16u;
-        uint32_t todo = __ballot_sync(0xffffffffu, loader && h >= 0);
-        while (todo) {
-            const int l = __ffs((int)todo) - 1;
-            todo &= todo - 1u;
-            const uint32_t pg = __shfl_sync(0xffffffffu, page, l);
-            const int32_t fr = __shfl_sync(0xffffffffu, h, l);
-            const int4* src = reinterpret_cast<const int4*>(b.backing + (size_t)pg * b.frame_size);
-            int4* dst = reinterpret_cast<int4*>(b.frames + (size_t)fr * b.frame_size);
-            for (uint32_t j = lane; j < n16; j += 32u) dst[j] = src[j];
+        const uint32_t todo = __ballot_sync(0xffffffffu, loader && h >= 0);
+        const uint32_t total = (uint32_t)__popc(todo) * n16;
+        for (uint32_t base = 0; base < total; base += 32u * kCopyInFlight) {
+            int4 v[kCopyInFlight];
+            int4* dst[kCopyInFlight];
+#pragma unroll
+            for (uint32_t u = 0; u < kCopyInFlight; ++u) {
+                const uint32_t c = base + u * 32u + lane;
+                const uint32_t li = (c < total ? c : 0u) / n16;
+                const int l = (int)nth_set_bit(todo, (int)li);   // every lane shuffles
+                const uint32_t pg = __shfl_sync(0xffffffffu, page, l);
+                const int32_t fr = __shfl_sync(0xffffffffu, h, l);
+                const uint32_t j = c - li * n16;
+                dst[u] = nullptr;
+                if (c < total) {
+                    v[u] = reinterpret_cast<const int4*>(b.backing + (size_t)pg * b.frame_size)[j];
+                    dst[u] = reinterpret_cast<int4*>(b.frames + (size_t)(uint32_t)fr * b.frame_size) + j;
+                }
+            }
+#pragma unroll
+            for (uint32_t u = 0; u < kCopyInFlight; ++u)
+                if (dst[u]) *dst[u] = v[u];
         }
         __syncwarp();
     }
@@ -476,7 +495,7 @@ __device__ __forceinline__ uint32_t merge_insert(uint32_t* keys, uint32_t* cnt, 
 // round may land after other blocks' fetches of the same round; a sweep
 // that meets a page whose release has not landed yet passes it as pinned,
 // as it would any pinned page.
-template <bool DIST, bool BYPAGE>
+template <bool DIST, bool BYPAGE, bool COPY>
 __device__ __forceinline__ void round_blocks(const BmView& b, const int32_t* release_of, const int32_t* release_idx,
                                              uint32_t n_release, const int32_t* pages, uint32_t n, uint32_t slot0,
                                              int32_t* frames_out, int32_t* held_out, unsigned long long& ok,
@@ -566,12 +585,12 @@ __device__ __forceinline__ void round_blocks(const BmView& b, const int32_t* rel
             const uint32_t lm = __ballot_sync(0xffffffffu, st == kStLoad);
             uint32_t old_page = kEmptyPage;
             const int32_t h = sweep_warp(b, lm, (uint32_t)p, &old_page, &w0);
-            if (lm) finish_loads_warp(b, st == kStLoad, (uint32_t)p, h, old_page, k, acc);
+            if (lm) finish_loads_warp<COPY>(b, st == kStLoad, (uint32_t)p, h, old_page, k, acc);
             if (st == kStLoad) f = h;
         } else if (st == kStLoad) {
             uint32_t old_page = kEmptyPage;
             const int32_t h = sweep_private(b, (uint32_t)p, slot, &old_page);
-            if (h >= 0 && b.backing && b.frames) copy_frame(b, (uint32_t)p, h);
+            if (COPY && h >= 0) copy_frame(b, (uint32_t)p, h);
             publish(b, (uint32_t)p, h, old_page, k, acc);
             f = h;
         }
@@ -604,9 +623,10 @@ __device__ __forceinline__ void round_blocks(const BmView& b, const int32_t* rel
 // One round: release the listed pins, then fetch this round's pages.
 // With one thread this is the deterministic replay of the round.
 // DIST: per-slot hands (b.dist), else the single shared hand.  BYPAGE:
-// release_of names pages, else frames.  held_out (may be null) receives
-// each fetch's page, or -1 where the fetch got no frame.
-template <bool DIST, bool BYPAGE>
+// release_of names pages, else frames.  COPY: misses copy their page from
+// the backing store (b.backing and b.frames set).  held_out (may be null)
+// receives each fetch's page, or -1 where the fetch got no frame.
+template <bool DIST, bool BYPAGE, bool COPY>
 __global__ void __launch_bounds__(256) k_round(BmView b, const int32_t* release_of, const int32_t* release_idx,
                                                uint32_t n_release, const int32_t* pages, uint32_t n, uint32_t slot0,
                                                int32_t* frames_out, int32_t* held_out) {
@@ -628,7 +648,7 @@ __global__ void __launch_bounds__(256) k_round(BmView b, const int32_t* release_
             if (held_out) held_out[i] = f >= 0 ? p : -1;
         }
     } else {
-        round_blocks<DIST, BYPAGE>(b, release_of, release_idx, n_release, pages, n, slot0, frames_out, held_out, ok,
+        round_blocks<DIST, BYPAGE, COPY>(b, release_of, release_idx, n_release, pages, n, slot0, frames_out, held_out, ok,
                                    bad, acc);
     }
     block_add_counters<7>({ok, bad, acc.hits, acc.misses, acc.evictions, acc.failures, acc.timeouts},
@@ -790,10 +810,18 @@ int launch_round(pbm_bufmgr* m, bool by_page, const int32_t* d_release_of, const
         kernel<<<grid, block, 0, s>>>(m->v, d_release_of, d_release_idx, n_release, d_pages, n, slot0, d_frames_out,
                                       d_held_out);
     };
-    if (m->v.dist)
-        by_page ? go(k_round<true, true>) : go(k_round<true, false>);
-    else
-        by_page ? go(k_round<false, true>) : go(k_round<false, false>);
+    const bool copy = m->v.backing && m->v.frames;
+    if (copy) {
+        if (m->v.dist)
+            by_page ? go(k_round<true, true, true>) : go(k_round<true, false, true>);
+        else
+            by_page ? go(k_round<false, true, true>) : go(k_round<false, false, true>);
+    } else {
+        if (m->v.dist)
+            by_page ? go(k_round<true, true, false>) : go(k_round<true, false, false>);
+        else
+            by_page ? go(k_round<false, true, false>) : go(k_round<false, false, false>);
+    }
     PBM_LAUNCH_CHECK();
     return PBM_OK;
 }

@@ -846,10 +846,15 @@ def config_buffer_manager(torch, pbm, stream, flush, n_fetch=1 << 26, round_size
     out = {"fetches": n_fetch, "round_size": round_size, "trace_gen_s": gen_s, "unit": "fetches/s",
            "l2": "flushed before every round"}
     # by_page: pins released by page (pbm_bufmgr_round_pages, release list
-    # naming the held-page array the rounds write), else by frame
-    runs = [("single_clock", pbm.BM_SINGLE_CLOCK, 1, 0, False), ("dist_clock", pbm.BM_DIST_CLOCK, 4096, 0, False),
+    # naming the held-page array the rounds write), else by frame.  The
+    # distributed clock gets one arm per request of a round, as the
+    # reference's arms are one per thread; 4096 arms shared by a round's
+    # 2^18 requests shows what sharing arms costs
+    runs = [("single_clock", pbm.BM_SINGLE_CLOCK, 1, 0, False),
+            ("dist_clock", pbm.BM_DIST_CLOCK, round_size, 0, False),
             ("single_clock_by_page", pbm.BM_SINGLE_CLOCK, 1, 0, True),
-            ("dist_clock_by_page", pbm.BM_DIST_CLOCK, 4096, 0, True),
+            ("dist_clock_by_page", pbm.BM_DIST_CLOCK, round_size, 0, True),
+            ("dist_clock_4096_arms", pbm.BM_DIST_CLOCK, 4096, 0, False),
             ("single_clock_copy4k", pbm.BM_SINGLE_CLOCK, 1, 4096, False)]
     backing = None
     d_held = torch.empty(n_fetch, dtype=torch.int32, device="cuda")

@@ -10,12 +10,15 @@
 //               its warps pull 32-request chunks of the block's range from a
 //               shared counter, finding a chunk's group by a ballot search of
 //               the prefix sums;
-//   graph       the persistent form captured once in a CUDA graph; the last
-//               block to finish advances the device-resident step counter, so
-//               each replay is one launch that reads the next step's
-//               descriptors from device memory.
+//   graph       the persistent form captured once in a CUDA graph; each block
+//               keeps its own device-resident replay counter (the grid is the
+//               same on every replay), so each replay is one launch that reads
+//               the next step's descriptors from device memory, and the last
+//               tenth of a step's chunks sits in pools that blocks which
+//               finish their own range early drain.
 #include <atomic>
 #include <type_traits>
+#include <vector>
 
 #include "batch_common.cuh"
 
@@ -31,7 +34,7 @@ struct BatchArgs {
     PoolView v;
     const pbm_group* groups;            // base of the descriptor table
     uint32_t n_groups;
-    uint32_t* d_step;                   // graph form: replay counter (may be null)
+    uint32_t* d_step;                   // graph form: per-block replay counters, one per block (may be null)
     uint32_t n_steps;                   // graph form: descriptor tables (replay k uses k mod n_steps)
     uint32_t seed;
     int32_t* arena;
@@ -40,7 +43,7 @@ struct BatchArgs {
     int32_t* results;                   // per request q (request order), may be null or host-mapped
     const unsigned long long* prefix;   // persistent, not fused: n_groups + 1 exclusive prefix
     int32_t fuse;                       // persistent: each block scans the groups itself
-    uint32_t* done;                     // graph form: blocks finished (last one advances d_step)
+    unsigned long long* pools;          // graph form: 2 x kPools tail-pool counters, 16 words apart (may be null)
     uint32_t max_steps;
     uint32_t stride;
     int32_t dedupe;
@@ -73,6 +76,48 @@ __device__ __forceinline__ void flush_bacc(const BAcc& a, DevStats* st) {
     block_add_counters<4>({a.ok, a.fail, a.steps, a.frees},
                           {&st->successes, &st->failures, &st->steps, &st->frees});
 }
+
+// The persistent kernel's end, with no block barrier: each warp adds its
+// sums into the block's shared counters (zeroed before the block's first
+// barrier) and counts itself done; the last warp of the block adds the
+// block's sums to the pool's counters.  Warps leave as soon as they are done.
+__device__ __forceinline__ void flush_bacc_last_warp(const BAcc& a, DevStats* st, unsigned long long* s_acc,
+                                                     unsigned int* s_warps_done) {
+    const uint32_t lane = threadIdx.x & 31u;
+    unsigned long long v[4] = {a.ok, a.fail, a.steps, a.frees};
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+#pragma unroll
+        for (int d = 16; d > 0; d >>= 1) v[k] += __shfl_down_sync(0xffffffffu, v[k], d);
+    }
+    unsigned int last = 0u;
+    if (lane == 0u) {
+#pragma unroll
+        for (int k = 0; k < 4; ++k)
+            if (v[k]) atomicAdd(s_acc + k, v[k]);
+        __threadfence_block();
+        last = atomicAdd(s_warps_done, 1u) == (blockDim.x >> 5) - 1u;
+    }
+    last = __shfl_sync(0xffffffffu, last, 0);
+    if (last) {
+        __threadfence_block();
+        if (lane < 4u) {
+            const unsigned long long x = atomicAdd(s_acc + lane, 0ull);   // every warp's sums
+            unsigned long long* dst = lane == 0u ? &st->successes
+                                    : lane == 1u ? &st->failures
+                                    : lane == 2u ? &st->steps : &st->frees;
+            if (x) atomicAdd(dst, x);
+        }
+    }
+}
+
+// The graph form's tail pools: the last 1/kPoolShare of a step's chunks,
+// split into kPools ranges; block b drains pool b mod kPools once its own
+// range is done.  Counters of replay k live at parity k & 1, so block 0 of
+// replay k clears the parity replay k + 1 will use (replay k - 1 has
+// finished with it).
+constexpr uint32_t kPools = 8;
+constexpr unsigned long long kPoolShare = 10;
 
 // The request's result: arena update, counters, and the free of the page it
 // gave up (merged per word within the warp when asked); converged call.
@@ -165,23 +210,31 @@ __device__ __forceinline__ uint32_t find_group_warp(const unsigned long long* pr
 
 // The persistent batch kernel.  With a.fuse each block scans the step's
 // group counts into shared memory itself (no separate prefix kernel); with
-// a.done the last block to finish advances the graph's step counter (no
-// separate step kernel), so one graph replay is one launch.  A warp serves
-// 32 requests (a chunk) at a time.  Each block owns a contiguous range of the
-// step's chunks and its warps take the next one from a shared-memory counter,
-// so a warp whose chunks needed extra jumps does not hold the block's end
-// back (static striding left the slowest of ~8 chunks per warp as the tail).
+// a.d_step each block reads and advances its own replay counter (no separate
+// step kernel, and no grid-wide "last block" atomic at the end), so one graph
+// replay is one launch.  A warp serves 32 requests (a chunk; 64 for Collab2)
+// at a time.  Each block owns a contiguous range of the step's chunks and its
+// warps take the next one from a shared-memory counter, so a warp whose
+// chunks needed extra jumps does not hold the block's end back (static
+// striding left the slowest of ~8 chunks per warp as the tail); with
+// a.pools, blocks that finish their range early then drain the tail pools
+// (one global counter per eighth of the grid, so no counter is hot).
 // (Prefetching the next chunk's arena slots and bitmap line into L2 was
 // measured slower: the extra instructions cost more than the latency they hid.)
 template <BWalk K, int W, typename Word, int MINB, typename Tab>
 __global__ void __launch_bounds__(256, MINB) k_batch_persistent(BatchArgs a, const __grid_constant__ Tab tab) {
     extern __shared__ unsigned long long s_prefix[];
     __shared__ int32_t slots[256];
-    __shared__ bool s_last;
-    __shared__ unsigned int s_next_chunk;
+    __shared__ unsigned long long s_acc[4];
+    __shared__ unsigned long long s_pool[2];   // the block's tail pool: first chunk, end
+    __shared__ unsigned int s_next_chunk, s_warps_done;
     BAcc acc;
-    if (threadIdx.x == 0) s_next_chunk = 0u;
-    const uint32_t step = a.d_step ? *a.d_step : 0u;
+    if (threadIdx.x == 0) {
+        s_next_chunk = 0u;
+        s_warps_done = 0u;
+    }
+    if (threadIdx.x < 4u) s_acc[threadIdx.x] = 0ull;
+    const uint32_t step = a.d_step ? a.d_step[blockIdx.x] : 0u;
     const pbm_group* groups;
     if constexpr (std::is_same<Tab, GroupTable>::value) groups = tab.g;   // read in place
     else groups = a.groups + (a.d_step ? (size_t)(step % a.n_steps) * a.n_groups : 0);
@@ -193,6 +246,10 @@ __global__ void __launch_bounds__(256, MINB) k_batch_persistent(BatchArgs a, con
     } else {
         __syncthreads();
     }
+    // every thread has read the block's replay counter: count this replay
+    if (a.d_step && threadIdx.x == 0) a.d_step[blockIdx.x] = step + 1u;
+    if (a.pools && blockIdx.x == 0 && threadIdx.x < kPools)
+        a.pools[(((step + 1u) & 1u) * kPools + threadIdx.x) * 16u] = 0ull;
     const unsigned long long total = pre[a.n_groups];
     const uint32_t lane = threadIdx.x & 31u;
     const uint32_t gl = threadIdx.x & (uint32_t)(W - 1);
@@ -201,7 +258,21 @@ __global__ void __launch_bounds__(256, MINB) k_batch_persistent(BatchArgs a, con
     volatile int32_t* gslots = slots + (threadIdx.x & ~(uint32_t)(W - 1));
     constexpr unsigned long long CH = 32ull * kReqPerLane<K>;    // requests per chunk
     const unsigned long long n_chunks = (total + CH - 1ull) / CH;
-    const unsigned long long per_block = (n_chunks + gridDim.x - 1ull) / gridDim.x;
+    // the block's own range; with pools, the last tenth goes to the pools
+    // (their bounds wait in shared memory until the range is done)
+    unsigned long long per_block;
+    if (a.pools) {
+        per_block = (n_chunks - n_chunks / kPoolShare) / gridDim.x;
+        if (threadIdx.x == 0) {
+            const unsigned long long pool0 = per_block * gridDim.x;
+            const unsigned long long psz = (n_chunks - pool0 + kPools - 1ull) / kPools;
+            s_pool[0] = pool0 + (blockIdx.x % kPools) * psz;
+            s_pool[1] = min(n_chunks, s_pool[0] + psz);
+        }
+        __syncthreads();
+    } else {
+        per_block = (n_chunks + gridDim.x - 1ull) / gridDim.x;
+    }
     const unsigned long long c_begin = (unsigned long long)blockIdx.x * per_block;
     const unsigned long long c_end = min(n_chunks, c_begin + per_block);
     // the group of the warp's previous chunk: chunks only grow and a group
@@ -211,8 +282,16 @@ __global__ void __launch_bounds__(256, MINB) k_batch_persistent(BatchArgs a, con
         uint32_t k = 0;
         if (lane == 0) k = atomicAdd(&s_next_chunk, 1u);
         k = __shfl_sync(0xffffffffu, k, 0);
-        const unsigned long long chunk = c_begin + k;
-        if (chunk >= c_end) break;
+        unsigned long long chunk = c_begin + k;
+        if (chunk >= c_end) {
+            // own range done: the pool's chunks (they follow every range,
+            // so the warp's chunks still only grow)
+            if (!a.pools) break;
+            unsigned long long j = 0;
+            if (lane == 0) j = atomicAdd(a.pools + ((step & 1u) * kPools + blockIdx.x % kPools) * 16u, 1ull);
+            chunk = s_pool[0] + __shfl_sync(0xffffffffu, j, 0);
+            if (chunk >= s_pool[1]) break;
+        }
         const unsigned long long q0 = chunk * CH;
         if (q0 >= pre[g0 + 1u]) g0 = find_group_warp(pre, a.n_groups, q0, g0);
         const unsigned long long g0_end = pre[g0 + 1u];
@@ -255,20 +334,7 @@ __global__ void __launch_bounds__(256, MINB) k_batch_persistent(BatchArgs a, con
             batch_round<K, W, Word>(a, seed, active, op, q, slot, lane_off, gslots, acc);
         }
     }
-    flush_bacc(acc, a.stats);
-    if (a.done) {
-        // every block read the step above; the last one to finish advances it
-        if (threadIdx.x == 0) {
-            __threadfence();
-            s_last = atomicAdd(a.done, 1u) == gridDim.x - 1u;
-        }
-        __syncthreads();
-        if (s_last && threadIdx.x == 0) {
-            *a.done = 0u;
-            *a.d_step = step + 1u;
-            __threadfence();
-        }
-    }
+    flush_bacc_last_warp(acc, a.stats, s_acc, &s_warps_done);
 }
 
 template <BWalk K, int W, typename Word>
@@ -563,19 +629,23 @@ int pbm_batch_graph_create_results(pbm_pool* pool, const pbm_walk_config* cfg, c
     g->graph = nullptr;
     g->exec = nullptr;
     g->d_step = nullptr;
-    g->d_done = nullptr;
+    g->d_pools = nullptr;
     g->d_prefix = nullptr;
-    if (cudaMalloc(&g->d_step, sizeof(uint32_t)) != cudaSuccess ||
-        cudaMalloc(&g->d_done, sizeof(uint32_t)) != cudaSuccess ||
+    // one replay counter per block of the persistent launch (its grid is
+    // fixed once the occupancy is resolved), and the tail pools' counters
+    g->n_step_slots = (uint32_t)(sm_count() * resolve_blocks_per_sm(cfg));
+    const size_t pool_bytes = sizeof(unsigned long long) * 2u * kPools * 16u;
+    if (cudaMalloc(&g->d_step, sizeof(uint32_t) * g->n_step_slots) != cudaSuccess ||
+        cudaMalloc(&g->d_pools, pool_bytes) != cudaSuccess ||
         cudaMalloc(&g->d_prefix, sizeof(unsigned long long) * (n_groups + 1u)) != cudaSuccess) {
         cudaGetLastError();
         cudaFree(g->d_step);
-        cudaFree(g->d_done);
+        cudaFree(g->d_pools);
         delete g;
         return PBM_ERR_NOMEM;
     }
-    PBM_CUDA_TRY(cudaMemsetAsync(g->d_step, 0, sizeof(uint32_t), s));
-    PBM_CUDA_TRY(cudaMemsetAsync(g->d_done, 0, sizeof(uint32_t), s));
+    PBM_CUDA_TRY(cudaMemsetAsync(g->d_step, 0, sizeof(uint32_t) * g->n_step_slots, s));
+    PBM_CUDA_TRY(cudaMemsetAsync(g->d_pools, 0, pool_bytes, s));
     PBM_CUDA_TRY(cudaStreamSynchronize(s));
     BatchArgs a = base_args(pool, cfg, d_arena, arena_len, seed0, nullptr);
     a.results = results;
@@ -584,7 +654,7 @@ int pbm_batch_graph_create_results(pbm_pool* pool, const pbm_walk_config* cfg, c
     a.prefix = g->d_prefix;
     a.d_step = g->d_step;
     a.n_steps = n_steps;
-    a.done = g->d_done;                       // the last block advances the step
+    a.pools = g->d_pools;
     a.fuse = n_groups <= kFusedGroups ? 1 : 0;
     // Capture on a private stream (the legacy default stream cannot be
     // captured); the graph is replayed later on the caller's stream.  The
@@ -599,6 +669,7 @@ int pbm_batch_graph_create_results(pbm_pool* pool, const pbm_walk_config* cfg, c
         cudaGetLastError();
         cudaStreamDestroy(cap);
         cudaFree(g->d_step);
+        cudaFree(g->d_pools);
         cudaFree(g->d_prefix);
         delete g;
         return PBM_ERR_CUDA;
@@ -607,13 +678,14 @@ int pbm_batch_graph_create_results(pbm_pool* pool, const pbm_walk_config* cfg, c
         k_batch_prefix<<<1, 1024, 0, cap>>>(d_groups, n_groups, g->d_step, n_steps, g->d_prefix);
         count_launch();
     }
-    rc = launch_batch(&c2, a, true, cap);
+    rc = launch_batch(&c2, a, true, cap, nullptr, g->n_step_slots);   // never more blocks than counters
     cudaGraph_t graph = nullptr;
     e = cudaStreamEndCapture(cap, &graph);
     cudaStreamDestroy(cap);
     if (rc || e != cudaSuccess) {
         if (graph) cudaGraphDestroy(graph);
         cudaFree(g->d_step);
+        cudaFree(g->d_pools);
         cudaFree(g->d_prefix);
         delete g;
         cudaGetLastError();
@@ -623,6 +695,7 @@ int pbm_batch_graph_create_results(pbm_pool* pool, const pbm_walk_config* cfg, c
     if (cudaGraphInstantiate(&g->exec, graph, 0) != cudaSuccess) {
         cudaGraphDestroy(graph);
         cudaFree(g->d_step);
+        cudaFree(g->d_pools);
         cudaFree(g->d_prefix);
         delete g;
         cudaGetLastError();
@@ -647,8 +720,12 @@ int pbm_graph_replay(pbm_graph* g, void* stream) {
 int pbm_graph_set_step(pbm_graph* g, uint32_t step, void* stream) {
     if (!g) return PBM_ERR_INVALID;
     pbm::DeviceScope scope(g->device);
-    PBM_CUDA_TRY(cudaMemcpyAsync(g->d_step, &step, sizeof(step), cudaMemcpyHostToDevice, (cudaStream_t)stream));
-    PBM_CUDA_TRY(cudaStreamSynchronize((cudaStream_t)stream));
+    cudaStream_t s = (cudaStream_t)stream;
+    std::vector<uint32_t> steps(g->n_step_slots ? g->n_step_slots : 1u, step);
+    PBM_CUDA_TRY(cudaMemcpyAsync(g->d_step, steps.data(), sizeof(uint32_t) * steps.size(), cudaMemcpyHostToDevice, s));
+    if (g->d_pools)
+        PBM_CUDA_TRY(cudaMemsetAsync(g->d_pools, 0, sizeof(unsigned long long) * 2u * kPools * 16u, s));
+    PBM_CUDA_TRY(cudaStreamSynchronize(s));
     return PBM_OK;
 }
 
@@ -658,7 +735,7 @@ int pbm_graph_destroy(pbm_graph* g) {
     if (g->exec) cudaGraphExecDestroy(g->exec);
     if (g->graph) cudaGraphDestroy(g->graph);
     cudaFree(g->d_step);
-    cudaFree(g->d_done);
+    cudaFree(g->d_pools);
     cudaFree(g->d_prefix);
     delete g;
     return PBM_OK;

@@ -91,8 +91,9 @@ __global__ void k_step_advance(uint32_t* d_step) {
 struct pbm_graph {
     cudaGraph_t graph;
     cudaGraphExec_t exec;
-    uint32_t* d_step;
-    uint32_t* d_done;                 // blocks finished in the current replay
+    uint32_t* d_step;                 // replay counter(s): one, or one per block of the batch kernel
+    uint32_t n_step_slots;            // entries of d_step
+    unsigned long long* d_pools;      // the batch kernel's tail-pool counters (may be null)
     unsigned long long* d_prefix;
     unsigned long long launches_per_replay;
     int device;                       // the pool's device: replays run there

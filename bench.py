@@ -139,15 +139,17 @@ def env_rank():
     return r, w, lr
 
 
-WALKS = ("collab32c", "pair32c", "collab32", "collab64c", "word32", "word64", "page")
+WALKS = ("collab32c", "pair32c", "pair32c6", "collab32", "collab64c", "word32", "word64", "page")
 
 
 def named_walk(pbm, name):
     """Walk configurations by name (`--walk`); the `c` forms are the
     register-capped kernels at 5 blocks per SM, all with unmerged frees;
-    `pair32c` serves two requests per lane (64 per warp, collab_width 64)."""
+    `pair32c` serves two requests per lane (64 per warp, collab_width 64),
+    `pair32c6` the same at 6 blocks per SM where the registers allow."""
     return {"collab32c": pbm.walk_config(pbm.COLLAB_RW_BM, word_bits=32, collab_width=32, blocks_per_sm=5),
             "pair32c": pbm.walk_config(pbm.COLLAB_RW_BM, word_bits=32, collab_width=64, blocks_per_sm=5),
+            "pair32c6": pbm.walk_config(pbm.COLLAB_RW_BM, word_bits=32, collab_width=64, blocks_per_sm=6),
             "collab32": pbm.walk_config(pbm.COLLAB_RW_BM, word_bits=32, collab_width=32),
             "collab64c": pbm.walk_config(pbm.COLLAB_RW_BM, word_bits=64, collab_width=32, blocks_per_sm=5),
             "word32": pbm.walk_config(pbm.RANDOM_WALK_BM, word_bits=32),
@@ -1284,6 +1286,7 @@ def run_profile_case(args):
     walk = {"collab32c": pbm.walk_config(pbm.COLLAB_RW_BM, word_bits=32, collab_width=32, blocks_per_sm=5,
                                          free_merge=0),
             "pair32c": pbm.walk_config(pbm.COLLAB_RW_BM, word_bits=32, collab_width=64, blocks_per_sm=5),
+            "pair32c6": pbm.walk_config(pbm.COLLAB_RW_BM, word_bits=32, collab_width=64, blocks_per_sm=6),
             "collab32": pbm.walk_config(pbm.COLLAB_RW_BM, word_bits=32, collab_width=32),
             "collab64": pbm.walk_config(pbm.COLLAB_RW_BM, word_bits=64, collab_width=32),
             "word32": pbm.walk_config(pbm.RANDOM_WALK_BM, word_bits=32)}[args.profile_walk]

@@ -10,13 +10,16 @@
 //               its warps pull 32-request chunks of the block's range from a
 //               shared counter, finding a chunk's group by a ballot search of
 //               the prefix sums;
-//   graph       the persistent form captured once in a CUDA graph; each block
-//               keeps its own device-resident replay counter (the grid is the
-//               same on every replay), so each replay is one launch that reads
-//               the next step's descriptors from device memory, and the last
-//               tenth of a step's chunks sits in pools that blocks which
-//               finish their own range early drain.
+//   graph       the persistent form captured once in a CUDA graph; the host
+//               counts the replays and writes the step into the kernel's
+//               parameters before each launch, so each replay is one launch
+//               that reads the step's descriptors from device memory with no
+//               counter to read first, and the last tenth of a step's chunks
+//               sits in pools that blocks which finish their own range early
+//               drain.
 #include <atomic>
+#include <new>
+#include <cstring>
 #include <type_traits>
 #include <vector>
 
@@ -34,8 +37,8 @@ struct BatchArgs {
     PoolView v;
     const pbm_group* groups;            // base of the descriptor table
     uint32_t n_groups;
-    uint32_t* d_step;                   // graph form: per-block replay counters, one per block (may be null)
-    uint32_t n_steps;                   // graph form: descriptor tables (replay k uses k mod n_steps)
+    uint32_t step;                      // graph form: the replay (set on the host before each launch)
+    uint32_t n_steps;                   // descriptor tables (replay k uses table k mod n_steps; >= 1)
     uint32_t seed;
     int32_t* arena;
     unsigned long long arena_len;
@@ -121,8 +124,9 @@ constexpr unsigned long long kPoolShare = 10;
 
 // The request's result: arena update, counters, and the free of the page it
 // gave up (merged per word within the warp when asked); converged call.
+template <typename SlotT>
 __device__ __forceinline__ void batch_finish(const BatchArgs& a, bool active, int op, unsigned long long q,
-                                             unsigned long long slot, int32_t held, bool need, int32_t id, int32_t s,
+                                             SlotT slot, int32_t held, bool need, int32_t id, int32_t s,
                                              BAcc& acc) {
     int32_t to_free = -1;
     if (active) {
@@ -171,10 +175,12 @@ __device__ __forceinline__ void batch_round(const BatchArgs& a, uint32_t seed, b
 }
 
 // Two requests per lane (a: q0 + lane, b: q0 + 32 + lane), one walk.
-template <typename Word>
+// SlotT: 32-bit arena slots when the arena has at most 2^31 of them (fewer
+// instructions per request), else 64-bit.
+template <typename Word, typename SlotT>
 __device__ __forceinline__ void batch_round2(const BatchArgs& a, uint32_t seed, unsigned long long q0,
-                                             bool act_a, int op_a, unsigned long long slot_a, bool act_b, int op_b,
-                                             unsigned long long slot_b, uint32_t lane_off, BAcc& acc) {
+                                             bool act_a, int op_a, SlotT slot_a, bool act_b, int op_b,
+                                             SlotT slot_b, uint32_t lane_off, BAcc& acc) {
     const bool need_a = act_a && (op_a == PBM_OP_ALLOC || op_a == PBM_OP_SWAP);
     const bool need_b = act_b && (op_b == PBM_OP_ALLOC || op_b == PBM_OP_SWAP);
     const int32_t held_a = (act_a && op_a != PBM_OP_ALLOC) ? a.arena[slot_a] : -1;
@@ -186,7 +192,8 @@ __device__ __forceinline__ void batch_round2(const BatchArgs& a, uint32_t seed, 
     batch_finish(a, act_b, op_b, q0 + 32u + (threadIdx.x & 31u), slot_b, held_b, need_b, id_b, s, acc);
 }
 
-__device__ __forceinline__ unsigned long long wrap_slot(unsigned long long slot, unsigned long long len) {
+template <typename S>
+__device__ __forceinline__ S wrap_slot(S slot, S len) {
     if (slot >= len) slot = slot - len < len ? slot - len : slot % len;
     return slot;
 }
@@ -209,9 +216,9 @@ __device__ __forceinline__ uint32_t find_group_warp(const unsigned long long* pr
 }
 
 // The persistent batch kernel.  With a.fuse each block scans the step's
-// group counts into shared memory itself (no separate prefix kernel); with
-// a.d_step each block reads and advances its own replay counter (no separate
-// step kernel, and no grid-wide "last block" atomic at the end), so one graph
+// group counts into shared memory itself (no separate prefix kernel); the
+// graph form's step comes with the launch's parameters (no counter to read,
+// no step kernel, no grid-wide "last block" atomic at the end), so one graph
 // replay is one launch.  A warp serves 32 requests (a chunk; 64 for Collab2)
 // at a time.  Each block owns a contiguous range of the step's chunks and its
 // warps take the next one from a shared-memory counter, so a warp whose
@@ -221,7 +228,7 @@ __device__ __forceinline__ uint32_t find_group_warp(const unsigned long long* pr
 // (one global counter per eighth of the grid, so no counter is hot).
 // (Prefetching the next chunk's arena slots and bitmap line into L2 was
 // measured slower: the extra instructions cost more than the latency they hid.)
-template <BWalk K, int W, typename Word, int MINB, typename Tab>
+template <BWalk K, int W, typename Word, int MINB, typename Tab, typename SlotT>
 __global__ void __launch_bounds__(256, MINB) k_batch_persistent(BatchArgs a, const __grid_constant__ Tab tab) {
     extern __shared__ unsigned long long s_prefix[];
     __shared__ int32_t slots[256];
@@ -234,10 +241,10 @@ __global__ void __launch_bounds__(256, MINB) k_batch_persistent(BatchArgs a, con
         s_warps_done = 0u;
     }
     if (threadIdx.x < 4u) s_acc[threadIdx.x] = 0ull;
-    const uint32_t step = a.d_step ? a.d_step[blockIdx.x] : 0u;
+    const uint32_t step = a.step;
     const pbm_group* groups;
     if constexpr (std::is_same<Tab, GroupTable>::value) groups = tab.g;   // read in place
-    else groups = a.groups + (a.d_step ? (size_t)(step % a.n_steps) * a.n_groups : 0);
+    else groups = a.groups + (size_t)(step % a.n_steps) * a.n_groups;
     const uint32_t seed = a.seed + step;
     const unsigned long long* pre = a.prefix;
     if (a.fuse) {
@@ -246,8 +253,6 @@ __global__ void __launch_bounds__(256, MINB) k_batch_persistent(BatchArgs a, con
     } else {
         __syncthreads();
     }
-    // every thread has read the block's replay counter: count this replay
-    if (a.d_step && threadIdx.x == 0) a.d_step[blockIdx.x] = step + 1u;
     if (a.pools && blockIdx.x == 0 && threadIdx.x < kPools)
         a.pools[(((step + 1u) & 1u) * kPools + threadIdx.x) * 16u] = 0ull;
     const unsigned long long total = pre[a.n_groups];
@@ -296,27 +301,29 @@ __global__ void __launch_bounds__(256, MINB) k_batch_persistent(BatchArgs a, con
         if (q0 >= pre[g0 + 1u]) g0 = find_group_warp(pre, a.n_groups, q0, g0);
         const unsigned long long g0_end = pre[g0 + 1u];
         // a chunk usually lies inside one group; requests past its end search on
-        auto locate = [&](unsigned long long q, int& op, unsigned long long& slot) {
+        auto locate = [&](unsigned long long q, int& op, SlotT& slot) {
             const uint32_t g = q < g0_end ? g0 : find_group_any(pre, a.n_groups, q, g0);
             const pbm_group gd = groups[g];
             op = gd.op;
-            slot = wrap_slot(gd.offset + (q - pre[g]), a.arena_len);
+            slot = (SlotT)wrap_slot<unsigned long long>(gd.offset + (q - pre[g]), a.arena_len);
         };
         const unsigned long long q = q0 + lane;
         bool active;
         int op = PBM_OP_ALLOC;
-        unsigned long long slot = 0;
+        SlotT slot = 0;
         if constexpr (K == BWalk::Collab2) {
             const unsigned long long qb = q + 32ull;
             bool act_b;
             int op_b = PBM_OP_ALLOC;
-            unsigned long long slot_b = 0;
+            SlotT slot_b = 0;
             if (q0 + CH <= g0_end) {
                 // the whole chunk lies in one group: its slots follow on from one base
+                // (base + 63 stays below 2^32 for 32-bit slots: the arena has at most 2^31)
                 const pbm_group gd = groups[g0];
-                const unsigned long long base = wrap_slot(gd.offset + (q0 - pre[g0]), a.arena_len);
-                slot = wrap_slot(base + lane, a.arena_len);
-                slot_b = wrap_slot(base + 32ull + lane, a.arena_len);
+                const SlotT len = (SlotT)a.arena_len;
+                const SlotT base = (SlotT)wrap_slot<unsigned long long>(gd.offset + (q0 - pre[g0]), a.arena_len);
+                slot = wrap_slot<SlotT>(base + (SlotT)lane, len);
+                slot_b = wrap_slot<SlotT>(base + (SlotT)(32u + lane), len);
                 op = gd.op;
                 op_b = gd.op;
                 active = true;
@@ -327,11 +334,11 @@ __global__ void __launch_bounds__(256, MINB) k_batch_persistent(BatchArgs a, con
                 if (active) locate(q, op, slot);
                 if (act_b) locate(qb, op_b, slot_b);
             }
-            batch_round2<Word>(a, seed, q0, active, op, slot, act_b, op_b, slot_b, lane_off, acc);
+            batch_round2<Word, SlotT>(a, seed, q0, active, op, slot, act_b, op_b, slot_b, lane_off, acc);
         } else {
             active = q < total;
             if (active) locate(q, op, slot);
-            batch_round<K, W, Word>(a, seed, active, op, q, slot, lane_off, gslots, acc);
+            batch_round<K, W, Word>(a, seed, active, op, q, (unsigned long long)slot, lane_off, gslots, acc);
         }
     }
     flush_bacc_last_warp(acc, a.stats, s_acc, &s_warps_done);
@@ -355,8 +362,8 @@ __global__ void __launch_bounds__(256) k_batch_plain(BatchArgs a) {
         const unsigned long long slot = wrap_slot(a.offset + ql, a.arena_len);
         if constexpr (K == BWalk::Collab2) {
             const bool act_b = ql + 32ull < a.count;
-            batch_round2<Word>(a, a.seed, a.q_base + chunk * CH, active, a.op, slot, act_b, a.op,
-                               wrap_slot(a.offset + ql + 32ull, a.arena_len), lane_off, acc);
+            batch_round2<Word, unsigned long long>(a, a.seed, a.q_base + chunk * CH, active, a.op, slot, act_b, a.op,
+                                                   wrap_slot(a.offset + ql + 32ull, a.arena_len), lane_off, acc);
         } else {
             batch_round<K, W, Word>(a, a.seed, active, a.op, a.q_base + ql, slot, lane_off, gslots, acc);
         }
@@ -374,13 +381,13 @@ namespace {
 // size, outside any stream capture).  The cache is one atomic word, (block
 // size << 16) | blocks, so host threads launching batches at once never read
 // a block size paired with another size's count.
-template <BWalk K, int W, typename Word, int MINB, typename Tab = NoTable>
+template <BWalk K, int W, typename Word, int MINB, typename Tab = NoTable, typename SlotT = unsigned long long>
 int persistent_blocks_per_sm(int block) {
     static std::atomic<uint32_t> cache{0u};
     const uint32_t c = cache.load(std::memory_order_relaxed);
     if ((int)(c >> 16) == block) return (int)(c & 0xffffu);
     int n = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_batch_persistent<K, W, Word, MINB, Tab>, block,
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_batch_persistent<K, W, Word, MINB, Tab, SlotT>, block,
                                                       kFusedPrefixBytes) != cudaSuccess) {
         cudaGetLastError();
         n = 1;
@@ -397,22 +404,40 @@ int persistent_blocks_per_sm(int block) {
 // collaborative walk on 32-bit words).
 // grid_cap > 0: at most that many blocks (a batch whose size the host knows
 // and that needs fewer blocks than fill the GPU).
-template <BWalk K, int W, typename Word, typename Tab>
-void launch_persistent(const BatchArgs& a, const Tab& tab, int block, int blocks_per_sm, size_t smem,
-                       cudaStream_t s, unsigned grid_cap) {
+template <BWalk K, int W, typename Word, typename Tab, typename SlotT>
+void launch_persistent_slots(const BatchArgs& a, const Tab& tab, int block, int blocks_per_sm, size_t smem,
+                             cudaStream_t s, unsigned grid_cap) {
     auto grid_of = [&](int per_sm) {
         const unsigned g = (unsigned)(sm_count() * per_sm);
         return grid_cap && grid_cap < g ? grid_cap : g;
     };
     if (blocks_per_sm >= kCappedBlocks) {
-        int fit = persistent_blocks_per_sm<K, W, Word, kCappedBlocks, Tab>(block);
+        int fit = persistent_blocks_per_sm<K, W, Word, kCappedBlocks, Tab, SlotT>(block);
         int per_sm = blocks_per_sm < fit ? blocks_per_sm : fit;
-        k_batch_persistent<K, W, Word, kCappedBlocks, Tab><<<grid_of(per_sm), block, smem, s>>>(a, tab);
+        k_batch_persistent<K, W, Word, kCappedBlocks, Tab, SlotT><<<grid_of(per_sm), block, smem, s>>>(a, tab);
     } else {
-        int fit = persistent_blocks_per_sm<K, W, Word, 1, Tab>(block);
+        int fit = persistent_blocks_per_sm<K, W, Word, 1, Tab, SlotT>(block);
         int per_sm = (blocks_per_sm > 0 && blocks_per_sm < fit) ? blocks_per_sm : fit;
-        k_batch_persistent<K, W, Word, 1, Tab><<<grid_of(per_sm), block, smem, s>>>(a, tab);
+        k_batch_persistent<K, W, Word, 1, Tab, SlotT><<<grid_of(per_sm), block, smem, s>>>(a, tab);
     }
+}
+
+// 32-bit arena slots for the two-requests-per-lane walk when the arena has at
+// most 2^31 slots; every other walk keeps 64-bit slots.
+constexpr unsigned long long kSlot32Max = 1ull << 31;
+
+template <BWalk K> constexpr bool kHasSlot32 = K == BWalk::Collab2;
+
+template <BWalk K, int W, typename Word, typename Tab>
+void launch_persistent(const BatchArgs& a, const Tab& tab, int block, int blocks_per_sm, size_t smem,
+                       cudaStream_t s, unsigned grid_cap) {
+    if constexpr (kHasSlot32<K>) {
+        if (a.arena_len <= kSlot32Max) {
+            launch_persistent_slots<K, W, Word, Tab, uint32_t>(a, tab, block, blocks_per_sm, smem, s, grid_cap);
+            return;
+        }
+    }
+    launch_persistent_slots<K, W, Word, Tab, unsigned long long>(a, tab, block, blocks_per_sm, smem, s, grid_cap);
 }
 
 // tab: the inline descriptor table of a launch-form batch (null: a.groups).
@@ -463,8 +488,9 @@ int launch_batch(const pbm_walk_config* c, const BatchArgs& a, bool persistent, 
 
 // Blocks per SM the persistent launch of this configuration will use
 // (resolved before a capture, so the capture issues no occupancy query).
-int resolve_blocks_per_sm(const pbm_walk_config* c) {
+int resolve_blocks_per_sm(const pbm_walk_config* c, unsigned long long arena_len) {
     const int block = c->block_size ? c->block_size : kDefaultBlock;
+    const bool slot32 = arena_len <= kSlot32Max;
     const bool w64 = c->word_bits == 64;
     const bool capped = c->blocks_per_sm >= kCappedBlocks;
     auto pick = [&](int fit1, int fitc) {
@@ -479,6 +505,11 @@ int resolve_blocks_per_sm(const pbm_walk_config* c) {
         return w64 ? PBM_FITS(BWalk::Word64, 32, uint64_t) : PBM_FITS(BWalk::Word32, 32, uint32_t);
     default: {
         const int W = c->collab_width ? c->collab_width : 32;
+        if (W == 64 && slot32)
+            return w64 ? pick(persistent_blocks_per_sm<BWalk::Collab2, 32, uint64_t, 1, NoTable, uint32_t>(block),
+                              persistent_blocks_per_sm<BWalk::Collab2, 32, uint64_t, kCappedBlocks, NoTable, uint32_t>(block))
+                       : pick(persistent_blocks_per_sm<BWalk::Collab2, 32, uint32_t, 1, NoTable, uint32_t>(block),
+                              persistent_blocks_per_sm<BWalk::Collab2, 32, uint32_t, kCappedBlocks, NoTable, uint32_t>(block));
         if (W == 64) return w64 ? PBM_FITS(BWalk::Collab2, 32, uint64_t) : PBM_FITS(BWalk::Collab2, 32, uint32_t);
         if (W == 8) return w64 ? PBM_FITS(BWalk::Collab, 8, uint64_t) : PBM_FITS(BWalk::Collab, 8, uint32_t);
         if (W == 16) return w64 ? PBM_FITS(BWalk::Collab, 16, uint64_t) : PBM_FITS(BWalk::Collab, 16, uint32_t);
@@ -500,6 +531,7 @@ BatchArgs base_args(pbm_pool* p, const pbm_walk_config* c, int32_t* arena, uint6
     a.stride = c->stride ? c->stride : 1u;
     a.merge = c->free_merge;
     a.stats = p->d_stats;
+    a.n_steps = 1u;
     const int Wc = c->strategy == PBM_COLLAB_RW_BM ? (c->collab_width ? c->collab_width : 32) : 1;
     const int W = Wc == 64 ? 32 : Wc;   // lanes reading the window
     const uint32_t L = c->word_bits == 64 ? p->view.n_words64 : p->view.n_words32;
@@ -589,7 +621,7 @@ int pbm_batch_launch_results(pbm_pool* pool, const pbm_walk_config* cfg, const p
         }
         pool->prefix_cap = n_groups + 1u;
     }
-    k_batch_prefix<<<1, 1024, 0, s>>>(d_groups, n_groups, nullptr, 1u, pool->d_prefix);
+    k_batch_prefix<<<1, 1024, 0, s>>>(d_groups, n_groups, nullptr, 0u, 1u, pool->d_prefix);
     PBM_LAUNCH_CHECK();
     a.groups = d_groups;
     a.n_groups = n_groups;
@@ -624,83 +656,88 @@ int pbm_batch_graph_create_results(pbm_pool* pool, const pbm_walk_config* cfg, c
     if (rc) return rc;
     *out = nullptr;
     cudaStream_t s = (cudaStream_t)stream;
-    pbm_graph* g = new pbm_graph();
+    pbm_graph* g = new (std::nothrow) pbm_graph();   // value-initialised: null handles, step 0
+    if (!g) return PBM_ERR_NOMEM;
     g->device = pool->device;
-    g->graph = nullptr;
-    g->exec = nullptr;
-    g->d_step = nullptr;
-    g->d_pools = nullptr;
-    g->d_prefix = nullptr;
-    // one replay counter per block of the persistent launch (its grid is
-    // fixed once the occupancy is resolved), and the tail pools' counters
-    g->n_step_slots = (uint32_t)(sm_count() * resolve_blocks_per_sm(cfg));
     const size_t pool_bytes = sizeof(unsigned long long) * 2u * kPools * 16u;
-    if (cudaMalloc(&g->d_step, sizeof(uint32_t) * g->n_step_slots) != cudaSuccess ||
-        cudaMalloc(&g->d_pools, pool_bytes) != cudaSuccess ||
+    if (cudaMalloc(&g->d_pools, pool_bytes) != cudaSuccess ||
         cudaMalloc(&g->d_prefix, sizeof(unsigned long long) * (n_groups + 1u)) != cudaSuccess) {
         cudaGetLastError();
-        cudaFree(g->d_step);
         cudaFree(g->d_pools);
         delete g;
         return PBM_ERR_NOMEM;
     }
-    PBM_CUDA_TRY(cudaMemsetAsync(g->d_step, 0, sizeof(uint32_t) * g->n_step_slots, s));
-    PBM_CUDA_TRY(cudaMemsetAsync(g->d_pools, 0, pool_bytes, s));
-    PBM_CUDA_TRY(cudaStreamSynchronize(s));
+    auto fail = [&](int code) {
+        if (g->exec) cudaGraphExecDestroy(g->exec);
+        if (g->graph) cudaGraphDestroy(g->graph);
+        cudaFree(g->d_pools);
+        cudaFree(g->d_prefix);
+        delete g;
+        cudaGetLastError();
+        return code;
+    };
+    if (cudaMemsetAsync(g->d_pools, 0, pool_bytes, s) != cudaSuccess || cudaStreamSynchronize(s) != cudaSuccess)
+        return fail(PBM_ERR_CUDA);
     BatchArgs a = base_args(pool, cfg, d_arena, arena_len, seed0, nullptr);
     a.results = results;
     a.groups = d_groups;
     a.n_groups = n_groups;
     a.prefix = g->d_prefix;
-    a.d_step = g->d_step;
+    a.step = 0u;                              // written before each replay
     a.n_steps = n_steps;
     a.pools = g->d_pools;
     a.fuse = n_groups <= kFusedGroups ? 1 : 0;
+    static_assert(sizeof(BatchArgs) <= sizeof(g->batch_args), "graph keeps the kernel's arguments");
+    std::memcpy(g->batch_args, &a, sizeof(a));
+    g->prefix_groups = d_groups;
+    g->prefix_n_groups = n_groups;
+    g->prefix_n_steps = n_steps;
+    g->prefix_out = g->d_prefix;
     // Capture on a private stream (the legacy default stream cannot be
     // captured); the graph is replayed later on the caller's stream.  The
     // occupancy query runs before capture.
     pbm_walk_config c2 = *cfg;
-    resolve_blocks_per_sm(cfg);   // fills the occupancy caches before the capture starts
+    resolve_blocks_per_sm(cfg, arena_len);   // fills the occupancy caches before the capture starts
     cudaStream_t cap = nullptr;
-    PBM_CUDA_TRY(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
+    if (cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking) != cudaSuccess) return fail(PBM_ERR_CUDA);
     const unsigned long long before = g_launches.load();
     cudaError_t e = cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal);
     if (e != cudaSuccess) {
-        cudaGetLastError();
         cudaStreamDestroy(cap);
-        cudaFree(g->d_step);
-        cudaFree(g->d_pools);
-        cudaFree(g->d_prefix);
-        delete g;
-        return PBM_ERR_CUDA;
+        return fail(PBM_ERR_CUDA);
     }
     if (!a.fuse) {
-        k_batch_prefix<<<1, 1024, 0, cap>>>(d_groups, n_groups, g->d_step, n_steps, g->d_prefix);
+        k_batch_prefix<<<1, 1024, 0, cap>>>(d_groups, n_groups, nullptr, 0u, n_steps, g->d_prefix);
         count_launch();
     }
-    rc = launch_batch(&c2, a, true, cap, nullptr, g->n_step_slots);   // never more blocks than counters
+    rc = launch_batch(&c2, a, true, cap);
     cudaGraph_t graph = nullptr;
     e = cudaStreamEndCapture(cap, &graph);
     cudaStreamDestroy(cap);
-    if (rc || e != cudaSuccess) {
-        if (graph) cudaGraphDestroy(graph);
-        cudaFree(g->d_step);
-        cudaFree(g->d_pools);
-        cudaFree(g->d_prefix);
-        delete g;
-        cudaGetLastError();
-        return rc ? rc : PBM_ERR_CUDA;
-    }
     g->graph = graph;
-    if (cudaGraphInstantiate(&g->exec, graph, 0) != cudaSuccess) {
-        cudaGraphDestroy(graph);
-        cudaFree(g->d_step);
-        cudaFree(g->d_pools);
-        cudaFree(g->d_prefix);
-        delete g;
-        cudaGetLastError();
-        return PBM_ERR_CUDA;
+    if (rc || e != cudaSuccess) return fail(rc ? rc : PBM_ERR_CUDA);
+    // the kernel nodes whose parameters carry the step
+    size_t nn = 0;
+    if (cudaGraphGetNodes(graph, nullptr, &nn) != cudaSuccess) return fail(PBM_ERR_CUDA);
+    std::vector<cudaGraphNode_t> nodes(nn);
+    if (nn && cudaGraphGetNodes(graph, nodes.data(), &nn) != cudaSuccess) return fail(PBM_ERR_CUDA);
+    for (cudaGraphNode_t node : nodes) {
+        cudaGraphNodeType t;
+        cudaKernelNodeParams kp{};
+        if (cudaGraphNodeGetType(node, &t) != cudaSuccess || t != cudaGraphNodeTypeKernel) continue;
+        if (cudaGraphKernelNodeGetParams(node, &kp) != cudaSuccess) return fail(PBM_ERR_CUDA);
+        kp.kernelParams = nullptr;   // pointed into the graph; replays pass their own
+        kp.extra = nullptr;
+        if (kp.func == (void*)k_batch_prefix) {
+            g->prefix_node = node;
+            g->prefix_kp = kp;
+        } else {
+            g->batch_node = node;
+            g->batch_kp = kp;
+        }
     }
+    if (!g->batch_node || (!a.fuse && !g->prefix_node)) return fail(PBM_ERR_CUDA);
+    if (cudaGraphInstantiate(&g->exec, graph, 0) != cudaSuccess) return fail(PBM_ERR_CUDA);
     g->launches_per_replay = g_launches.load() - before;
     // capture does not launch: take the counted launches back
     g_launches.fetch_sub(g->launches_per_replay);
@@ -712,6 +749,29 @@ int pbm_batch_graph_create_results(pbm_pool* pool, const pbm_walk_config* cfg, c
 int pbm_graph_replay(pbm_graph* g, void* stream) {
     if (!g || !g->exec) return PBM_ERR_INVALID;
     pbm::DeviceScope scope(g->device);
+    if (g->batch_node) {
+        // this replay's step goes into the kernels' parameters (a host-side
+        // update of the instantiated graph; launches already queued keep theirs)
+        BatchArgs a;
+        std::memcpy(&a, g->batch_args, sizeof(a));
+        a.step = g->host_step;
+        NoTable tab{};
+        void* args[2] = {&a, &tab};
+        cudaKernelNodeParams kp = g->batch_kp;
+        kp.kernelParams = args;
+        PBM_CUDA_TRY(cudaGraphExecKernelNodeSetParams(g->exec, g->batch_node, &kp));
+        if (g->prefix_node) {
+            const pbm_group* groups = g->prefix_groups;
+            uint32_t n_groups = g->prefix_n_groups, step = g->host_step, n_steps = g->prefix_n_steps;
+            const uint32_t* no_counter = nullptr;
+            unsigned long long* prefix = g->prefix_out;
+            void* pargs[6] = {&groups, &n_groups, &no_counter, &step, &n_steps, &prefix};
+            cudaKernelNodeParams pkp = g->prefix_kp;
+            pkp.kernelParams = pargs;
+            PBM_CUDA_TRY(cudaGraphExecKernelNodeSetParams(g->exec, g->prefix_node, &pkp));
+        }
+        ++g->host_step;
+    }
     PBM_CUDA_TRY(cudaGraphLaunch(g->exec, (cudaStream_t)stream));
     count_launch(g->launches_per_replay);
     return PBM_OK;
@@ -721,10 +781,13 @@ int pbm_graph_set_step(pbm_graph* g, uint32_t step, void* stream) {
     if (!g) return PBM_ERR_INVALID;
     pbm::DeviceScope scope(g->device);
     cudaStream_t s = (cudaStream_t)stream;
-    std::vector<uint32_t> steps(g->n_step_slots ? g->n_step_slots : 1u, step);
-    PBM_CUDA_TRY(cudaMemcpyAsync(g->d_step, steps.data(), sizeof(uint32_t) * steps.size(), cudaMemcpyHostToDevice, s));
-    if (g->d_pools)
+    if (g->batch_node) {
+        g->host_step = step;
+        // both parities of the tail pools start empty again
         PBM_CUDA_TRY(cudaMemsetAsync(g->d_pools, 0, sizeof(unsigned long long) * 2u * kPools * 16u, s));
+    } else {
+        PBM_CUDA_TRY(cudaMemcpyAsync(g->d_step, &step, sizeof(step), cudaMemcpyHostToDevice, s));
+    }
     PBM_CUDA_TRY(cudaStreamSynchronize(s));
     return PBM_OK;
 }

@@ -73,12 +73,14 @@ __device__ __forceinline__ void block_exclusive_prefix(const pbm_group* g, uint3
 }
 
 // Exclusive prefix of one step's groups (one block of 1024 threads).
-// Graph forms keep a monotone replay counter; replay k reads descriptor table
-// k mod n_steps (so a graph may be replayed any number of times).
+// Graph forms keep a monotone replay counter -- in device memory (d_step) or
+// in the launch's parameters (step, when d_step is null); replay k reads
+// descriptor table k mod n_steps (so a graph may be replayed any number of
+// times).
 __global__ void k_batch_prefix(const pbm_group* groups, uint32_t n_groups, const uint32_t* d_step,
-                               uint32_t n_steps, unsigned long long* prefix) {
-    const uint32_t step = d_step ? *d_step % n_steps : 0u;
-    block_exclusive_prefix(groups + (size_t)step * n_groups, n_groups, prefix);
+                               uint32_t step, uint32_t n_steps, unsigned long long* prefix) {
+    const uint32_t k = (d_step ? *d_step : step) % (n_steps ? n_steps : 1u);
+    block_exclusive_prefix(groups + (size_t)k * n_groups, n_groups, prefix);
 }
 
 __global__ void k_step_advance(uint32_t* d_step) {
@@ -88,13 +90,25 @@ __global__ void k_step_advance(uint32_t* d_step) {
 }  // namespace
 }  // namespace pbm
 
+// A captured graph.  Its replay counter lives either in device memory
+// (d_step, advanced by a kernel of the graph) or on the host (host_step,
+// written into the kernels' parameters before each replay: the launches
+// then read the step with their parameters instead of from memory).
 struct pbm_graph {
     cudaGraph_t graph;
     cudaGraphExec_t exec;
-    uint32_t* d_step;                 // replay counter(s): one, or one per block of the batch kernel
-    uint32_t n_step_slots;            // entries of d_step
+    uint32_t* d_step;                 // device replay counter (null: host_step)
+    uint32_t host_step;
     unsigned long long* d_pools;      // the batch kernel's tail-pool counters (may be null)
     unsigned long long* d_prefix;
     unsigned long long launches_per_replay;
     int device;                       // the pool's device: replays run there
+    // host-counted form: the kernel nodes whose parameters carry the step,
+    // their launch settings, and the parameter values they were captured with
+    cudaGraphNode_t batch_node, prefix_node;
+    cudaKernelNodeParams batch_kp, prefix_kp;
+    alignas(16) unsigned char batch_args[256];
+    const pbm_group* prefix_groups;
+    uint32_t prefix_n_groups, prefix_n_steps;
+    unsigned long long* prefix_out;
 };

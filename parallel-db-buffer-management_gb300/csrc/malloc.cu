@@ -315,7 +315,7 @@ int batch_impl(pbm_pool* pool, bool queue, const pbm_group* d_groups, const pbm_
     }
     if ((mode != PBM_LAUNCH_PERSISTENT && mode != PBM_LAUNCH_SERIAL) || !d_groups) return PBM_ERR_INVALID;
     if (!ensure_prefix(t, n_groups)) return PBM_ERR_NOMEM;
-    k_batch_prefix<<<1, 1024, 0, s>>>(d_groups, n_groups, nullptr, 1u, t->prefix);
+    k_batch_prefix<<<1, 1024, 0, s>>>(d_groups, n_groups, nullptr, 0u, 1u, t->prefix);
     PBM_LAUNCH_CHECK();
     a.groups = d_groups;
     a.n_groups = n_groups;
@@ -374,7 +374,7 @@ int graph_impl(pbm_pool* pool, bool queue, const pbm_group* d_groups, uint32_t n
     PBM_CUDA_TRY(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
     cudaError_t e = cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal);
     if (e == cudaSuccess) {
-        k_batch_prefix<<<1, 1024, 0, cap>>>(d_groups, n_groups, g->d_step, n_steps, g->d_prefix);
+        k_batch_prefix<<<1, 1024, 0, cap>>>(d_groups, n_groups, g->d_step, 0u, n_steps, g->d_prefix);
         if (queue) k_malloc_persistent<false, true><<<sm_count() * per_sm, 256, 0, cap>>>(a);
         else k_malloc_persistent<false, false><<<sm_count() * per_sm, 256, 0, cap>>>(a);
         k_step_advance<<<1, 32, 0, cap>>>(g->d_step);

@@ -1097,7 +1097,12 @@ def run_profile_kernel(args):
     elif args.profile_kernel == "malloc":
         T, groups, rounds = 1 << 19, 32, 8
         pool = pbm.Pool(T, PAGE_SIZE, materialize=True)
-        pool.malloc_init()
+        queue = args.malloc_backend == "queue"
+        if queue:
+            pool.qmalloc_init(1 << 20)
+        else:
+            pool.malloc_init()
+        batch = pool.qmalloc_batch if queue else pool.malloc_batch
         rng = np.random.default_rng(4)
         counts = np.clip(np.floor(np.exp(rng.uniform(0, math.log(MAX_GROUP + 1), (rounds, groups)))), 1,
                          MAX_GROUP).astype(np.int64)
@@ -1120,8 +1125,8 @@ def run_profile_kernel(args):
             tab["offset"][groups:] = n_max + np.concatenate([[0], np.cumsum(prev_c)[:-1]])
             d_tab = torch.from_numpy(tab.view(np.uint8).copy()).cuda()
             flush.zero_()
-            pool.malloc_batch(d_tab, None, 2 * groups, sizes, ptrs, 2 * n_max, 77 + r, pbm.LAUNCH_PERSISTENT,
-                              max_steps=512, stream=sh)
+            batch(d_tab, None, 2 * groups, sizes, ptrs, 2 * n_max, 77 + r, pbm.LAUNCH_PERSISTENT, max_steps=512,
+                  stream=sh)
             ptrs[n_max:].zero_()
             ptrs[n_max:n_max + n].copy_(ptrs[:n])
             ptrs[:n_max].zero_()
@@ -1334,6 +1339,8 @@ def main():
                     help="--profile-kernel bufmgr: log2 of the frames (22 is the benchmark's buffer manager)")
     ap.add_argument("--bm-rounds", type=int, default=16,
                     help="--profile-kernel bufmgr: rounds of 2^18 fetches")
+    ap.add_argument("--malloc-backend", default="runs", choices=["runs", "queue"],
+                    help="--profile-kernel malloc: page runs (pbm_malloc_*) or per-class queues (pbm_qmalloc_*)")
     ap.add_argument("--bm-by-page", action="store_true",
                     help="--profile-kernel bufmgr: release pins by page (pbm_bufmgr_round_pages)")
     ap.add_argument("--configs", default="all",

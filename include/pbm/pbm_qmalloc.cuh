@@ -31,15 +31,19 @@ constexpr uint32_t kEmptyHandle = 0xffffffffu;
 constexpr uint32_t kQSpinLimit = 1u << 16;
 constexpr uint8_t kQCont = 0x80u;   // class_of mark of a chunk's pages after its first
 
+// Each counter sits in a 128-byte line of its own: every warp that mallocs
+// or frees a class touches its counters, and counters that shared a line
+// (or classes that shared one) queued their atomics at one L2 slice.
 struct QueueRing {
-    unsigned long long head;    // next dequeue ticket
-    unsigned long long tail;    // next enqueue ticket
-    unsigned long long avail;   // blocks published (signed, two's complement)
-    unsigned long long space;   // free slots (signed, two's complement)
+    alignas(128) unsigned long long head;    // next dequeue ticket
+    alignas(128) unsigned long long tail;    // next enqueue ticket
+    alignas(128) unsigned long long avail;   // blocks published (signed, two's complement)
+    alignas(128) unsigned long long space;   // free slots (signed, two's complement)
 };
 
-// counters[] indices
-constexpr int kQChunks = 0, kQOverflow = 1, kQTimeouts = 2, kQBadFrees = 3;
+// counters[] indices, one 128-byte line apart (kQCounterWords words in all)
+constexpr int kQChunks = 0, kQOverflow = 16, kQTimeouts = 32, kQBadFrees = 48;
+constexpr int kQCounterWords = 64;
 
 struct QMallocView {
     PoolView pool;

@@ -518,7 +518,7 @@ int pbm_qmalloc_init(pbm_pool* pool, uint32_t ring_capacity) {
     if (cudaMalloc(&t->rings, sizeof(QueueRing) * kQClasses) != cudaSuccess ||
         cudaMalloc(&t->slots, sizeof(uint32_t) * (size_t)kQClasses * cap) != cudaSuccess ||
         cudaMalloc(&t->class_of, n) != cudaSuccess ||
-        cudaMalloc(&t->qcounters, sizeof(unsigned long long) * 4) != cudaSuccess) {
+        cudaMalloc(&t->qcounters, sizeof(unsigned long long) * kQCounterWords) != cudaSuccess) {
         cudaGetLastError();
         free_queue(t);
         drop_if_empty(pool);
@@ -527,7 +527,7 @@ int pbm_qmalloc_init(pbm_pool* pool, uint32_t ring_capacity) {
     t->qcap = cap;
     PBM_CUDA_TRY(cudaMemset(t->slots, 0xff, sizeof(uint32_t) * (size_t)kQClasses * cap));
     PBM_CUDA_TRY(cudaMemset(t->class_of, 0, n));
-    PBM_CUDA_TRY(cudaMemset(t->qcounters, 0, sizeof(unsigned long long) * 4));
+    PBM_CUDA_TRY(cudaMemset(t->qcounters, 0, sizeof(unsigned long long) * kQCounterWords));
     k_qmalloc_init<<<1, 32>>>(t->rings, cap);
     PBM_LAUNCH_CHECK();
     PBM_CUDA_TRY(cudaDeviceSynchronize());
@@ -571,7 +571,7 @@ int pbm_qmalloc_counts(pbm_pool* pool, uint64_t* h_queued, uint64_t* h_chunks, u
     if (!t || !t->rings) return PBM_ERR_INVALID;
     cudaStream_t s = (cudaStream_t)stream;
     QueueRing r[kQClasses];
-    unsigned long long c[4];
+    unsigned long long c[kQCounterWords];
     PBM_CUDA_TRY(cudaMemcpyAsync(r, t->rings, sizeof(r), cudaMemcpyDeviceToHost, s));
     PBM_CUDA_TRY(cudaMemcpyAsync(c, t->qcounters, sizeof(c), cudaMemcpyDeviceToHost, s));
     PBM_CUDA_TRY(cudaStreamSynchronize(s));

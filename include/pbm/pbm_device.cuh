@@ -44,11 +44,12 @@ struct DevStats {
 
 // FIFO free list of the linked-list strategy: a ring of page ids with
 // ticket counters.  `avail` is a signed count stored in two's complement.
+// Every get and put of every thread hits these counters, so each has a
+// 128-byte line (an L2 slice's atomic unit) of its own.
 struct FifoState {
-    unsigned long long head;   // next get ticket
-    unsigned long long tail;   // next put ticket
-    unsigned long long avail;  // free pages in the ring
-    unsigned long long pad;
+    alignas(128) unsigned long long head;    // next get ticket
+    alignas(128) unsigned long long tail;    // next put ticket
+    alignas(128) unsigned long long avail;   // free pages in the ring
 };
 
 constexpr uint32_t kFifoSpinLimit = 1u << 20;   // bounded waits in the free list

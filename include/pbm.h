@@ -235,9 +235,13 @@ int pbm_batch_launch_results(pbm_pool *pool, const pbm_walk_config *cfg, const p
                              uint32_t seed, int32_t *d_steps, int32_t *results, int mode, void *stream);
 
 /* Graph-replayed persistent batch.  Replay k reads the descriptors at
- * d_groups + (k mod n_steps)*n_groups with seed seed0 + k, where k is a
- * device-resident counter that each replay advances (pbm_graph_set_step sets
- * it); replay with pbm_graph_replay, any number of times. */
+ * d_groups + (k mod n_steps)*n_groups with seed seed0 + k.  The batch graph
+ * counts its replays on the host: pbm_graph_replay writes k into the graph's
+ * kernel parameters before it launches (launches already queued keep their
+ * own k) and advances it; pbm_graph_set_step sets it.  Replay any number of
+ * times, from one host thread at a time and in stream order.  (The malloc
+ * graphs keep their counter in device memory and advance it with a kernel of
+ * the graph.) */
 typedef struct pbm_graph pbm_graph;
 int pbm_batch_graph_create(pbm_pool *pool, const pbm_walk_config *cfg, const pbm_group *d_groups,
                            uint32_t n_groups, uint32_t n_steps, int32_t *d_arena,

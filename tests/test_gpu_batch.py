@@ -103,6 +103,50 @@ def test_graph_replays_past_its_steps_wrap(cuda, pbm_mod, orc, fused):
     pool.close()
 
 
+@pytest.mark.parametrize("fused", [True, False])
+def test_graph_set_step_selects_the_table(cuda, pbm_mod, orc, fused):
+    """The graph's step lives on the host and travels in the kernels'
+    parameters: pbm_graph_set_step(k) makes the next replay read table
+    k mod n_steps, and every request of that table is served exactly once --
+    also the last tenth of the chunks, which the tail pools hand out (their
+    counters start empty again after set_step)."""
+    torch = cuda
+    pbm = pbm_mod
+    T, occ, seed = 1 << 20, 0.9, 2
+    n_groups = 64 if fused else 5000
+    pool = pbm.Pool(T, 64)
+    pool.prefill(occ, seed)
+    words, held = _held_arena(orc, T, occ, seed)
+    H = len(held)
+    arena = torch.from_numpy(held).cuda()
+    rng = np.random.default_rng(5)
+    hi = 4000 if fused else 60
+    counts = rng.integers(1, hi, size=(3, n_groups))
+    counts[1] //= 2   # three tables of different sizes
+    tab = np.concatenate([_descs(counts[s], pbm.OP_SWAP, int(counts[:s].sum()), H) for s in range(3)])
+    d_tab = torch.from_numpy(tab.view(np.uint8).copy()).cuda()
+    g = pool.graph(pbm.walk_config(pbm.COLLAB_RW_BM, collab_width=64, blocks_per_sm=5), d_tab, n_groups, 3,
+                   arena, H, 700)
+    done = 0
+    for step in (1, 0, 4, 2, 2):   # replay reads table step mod 3
+        g.set_step(step)
+        g.replay()
+        torch.cuda.synchronize()
+        done += int(counts[step % 3].sum())
+        st = pool.stats()
+        assert st.failures == 0 and st.successes == done == st.frees
+    # replays without set_step continue from the last step
+    g.replay()
+    torch.cuda.synchronize()
+    done += int(counts[0].sum())   # step 3 -> table 0
+    st = pool.stats()
+    assert st.successes == done == st.frees
+    g.close()
+    chk = pool.check(arena, H)
+    assert chk.n_duplicates == 0 and chk.n_not_marked == 0 and chk.used_pages == H
+    pool.close()
+
+
 def test_alloc_then_free_groups(cuda, pbm_mod, orc):
     """ALLOC groups fill an arena, FREE groups release it; mixed ops in one
     persistent batch keep the invariants and free restores the prefill."""

@@ -386,12 +386,20 @@ def run_ours(args, rank, world, local_rank):
     tab = build_descriptors(counts, H, pbm.OP_SWAP)
     d_tab = torch.from_numpy(tab.view(np.uint8).reshape(-1).copy()).to(dev)
     flush = torch.empty(512 << 20, dtype=torch.uint8, device=dev)
-    # autotuner (untimed): candidates run on step 0's groups, swaps keep the pool at 90%
+    # autotuner (untimed): candidates run on step 0's groups, swaps keep the
+    # pool at 90%.  It tunes a scratch copy of the pool (same prefill, same
+    # arena), so its few hundred passes of churn leave the measured pool as
+    # the workload defines it: prefilled, then the warm-up and timed steps
     tuned = []
     if args.walk == "auto":
-        tuned = pool.autotune(d_tab[:N_GROUPS * 16], N_GROUPS, int(counts[0].sum()), arena, H, seed=SEED0 - 999,
-                              reps=7, stream=sh)
+        scratch = pbm.Pool(T_PAGES, PAGE_SIZE, materialize=False)
+        scratch.prefill(OCCUPANCY, PREFILL_SEED, sh)
+        scratch_arena = arena.clone()
+        tuned = scratch.autotune(d_tab[:N_GROUPS * 16], N_GROUPS, int(counts[0].sum()), scratch_arena, H,
+                                 seed=SEED0 - 999, reps=7, stream=sh)
         torch.cuda.synchronize()
+        scratch.close()
+        del scratch_arena
     cfg = named_walk(pbm, "collab32c" if args.walk == "auto" else args.walk)
     if tuned:
         cfg = pbm.WalkConfig.from_buffer_copy(tuned[0].cfg)

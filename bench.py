@@ -1077,12 +1077,18 @@ def run_profile_kernel(args):
     out = {"profile_kernel": args.profile_kernel}
     if args.profile_kernel == "bufmgr":
         R, rounds = 1 << 18, args.bm_rounds
-        pages = workloads.zipf_pages(1 << 24, 0.99, R * rounds, 3)
+        n_logical = 1 << args.bm_logical_log2
+        pages = workloads.zipf_pages(n_logical, 0.99, R * rounds, 3)
         ptr, idx = workloads.release_lists(rounds, R, 0.25, 3)
         d_pages = torch.from_numpy(pages).cuda()
         d_idx = torch.from_numpy(idx).cuda()
         d_frames = torch.full((R * rounds,), -1, dtype=torch.int32, device="cuda")
-        bm = pbm.BufferManager(1 << 24, 1 << args.bm_frames_log2, policy=pbm.BM_SINGLE_CLOCK)
+        dist = args.bm_policy == "dist"
+        fsz = args.bm_frame_size
+        backing = torch.empty(n_logical * fsz // 4, dtype=torch.int32, device="cuda") if fsz else None
+        bm = pbm.BufferManager(n_logical, 1 << args.bm_frames_log2, frame_size=fsz,
+                               policy=pbm.BM_DIST_CLOCK if dist else pbm.BM_SINGLE_CLOCK, n_arms=R if dist else 1,
+                               backing=backing)
         d_held = torch.full((R * rounds,), -1, dtype=torch.int32, device="cuda")
         per_round = []
         for r in range(rounds):
@@ -1349,6 +1355,12 @@ def main():
                     help="--profile-kernel bufmgr: rounds of 2^18 fetches")
     ap.add_argument("--malloc-backend", default="runs", choices=["runs", "queue"],
                     help="--profile-kernel malloc: page runs (pbm_malloc_*) or per-class queues (pbm_qmalloc_*)")
+    ap.add_argument("--bm-logical-log2", type=int, default=24,
+                    help="--profile-kernel bufmgr: log2 of the logical pages (24 is the benchmark's)")
+    ap.add_argument("--bm-policy", default="single", choices=["single", "dist"],
+                    help="--profile-kernel bufmgr: one shared hand, or one private hand per request of a round")
+    ap.add_argument("--bm-frame-size", type=int, default=0,
+                    help="--profile-kernel bufmgr: bytes per frame copied from a backing store on a miss (0: none)")
     ap.add_argument("--bm-by-page", action="store_true",
                     help="--profile-kernel bufmgr: release pins by page (pbm_bufmgr_round_pages)")
     ap.add_argument("--configs", default="all",

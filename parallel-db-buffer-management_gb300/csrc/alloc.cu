@@ -232,7 +232,12 @@ __global__ void __launch_bounds__(256) k_claim_write_free(AllocArgs a, uint32_t 
         if (a.steps) a.steps[r] = s;
         if (id >= 0) {
             int32_t* pg = reinterpret_cast<int32_t*>(a.v.base + (size_t)(uint32_t)id * a.v.page_size);
-            for (uint32_t k = 0; k < payload_words; ++k) pg[k] = (int32_t)r;
+            uint32_t k = 0;
+            if (((a.v.page_size | (uint32_t)(uintptr_t)a.v.base) & 15u) == 0u) {   // 16-byte aligned pages: 16 bytes a store
+                const int4 v4 = make_int4((int32_t)r, (int32_t)r, (int32_t)r, (int32_t)r);
+                for (; k + 4u <= payload_words; k += 4u) *reinterpret_cast<int4*>(pg + k) = v4;
+            }
+            for (; k < payload_words; ++k) pg[k] = (int32_t)r;
             if (!hold) { free_page(a.v, id); ++frees; }
         }
         acc.ok += id >= 0;
@@ -470,8 +475,11 @@ int pbm_claim_write_free(pbm_pool* pool, uint32_t n, uint32_t seed, uint32_t pay
     c.strategy = PBM_RANDOM_WALK;
     c.max_steps = max_steps;
     AllocArgs a = make_args(pool, &c, n, seed, d_ids, d_steps);
-    int grid = (int)((n + 255u) / 256u);
-    k_claim_write_free<<<grid, 256, 0, (cudaStream_t)stream>>>(a, payload_bytes / 4u, hold);
+    // a batch too small to give every SM two 256-thread blocks runs in
+    // 64-thread blocks, so its walks spread over every SM
+    const int block = n < (uint32_t)sm_count() * 512u ? 64 : 256;
+    int grid = (int)((n + (uint32_t)block - 1u) / (uint32_t)block);
+    k_claim_write_free<<<grid, block, 0, (cudaStream_t)stream>>>(a, payload_bytes / 4u, hold);
     PBM_LAUNCH_CHECK();
     pool->fifo_valid = false;
     return PBM_OK;

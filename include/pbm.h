@@ -377,7 +377,9 @@ int pbm_bufmgr_reset(pbm_bufmgr *m, void *stream);
  * held is counted bad and undone; until it is undone, a fetch of the same
  * page may see it as pinned or, if the page is not resident, wait for it.
  * The lanes of a warp that release the same frame (or page) merge into one
- * release, which is rejected whole if it asks for more pins than are held. */
+ * release, which is rejected whole if it asks for more pins than are held.
+ * A round with releases and no fetches (n = 0) only unpins: the clock hand
+ * and the reference bits stay as they were. */
 int pbm_bufmgr_round(pbm_bufmgr *m, const int32_t *d_frames_of, const int32_t *d_release_idx,
                      uint32_t n_release, const int32_t *d_pages, uint32_t n, uint32_t slot0,
                      int32_t *d_frames_out, int serial, void *stream);

@@ -620,6 +620,29 @@ __device__ __forceinline__ void round_blocks(const BmView& b, const int32_t* rel
     }
 }
 
+// A round of releases only (no fetch): the lanes of a warp that release
+// one name merge into one atomic, and no sweep runs, so the hand stays where
+// it is.  BYPAGE as for k_round.
+template <bool BYPAGE>
+__global__ void __launch_bounds__(256, 4) k_release(BmView b, const int32_t* release_of, const int32_t* release_idx,
+                                                 uint32_t n_release) {
+    unsigned long long ok = 0, bad = 0;
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    // warp-uniform trip count (blockDim is a multiple of 32)
+    for (uint64_t base = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x - lane; base < n_release; base += stride) {
+        const uint64_t j = base + lane;
+        const int32_t rv = j < n_release ? __ldcg(release_of + __ldg(release_idx + j)) : -1;
+        const uint32_t peers = __match_any_sync(0xffffffffu, rv >= 0 ? (uint32_t)rv : 0x80000000u + lane);
+        uint32_t q = 0;
+        int32_t f = -1;
+        const uint32_t k = (uint32_t)__popc(peers);
+        if (rv >= 0 && (uint32_t)(__ffs((int)peers) - 1) == lane && release_target<BYPAGE>(b, rv, k, &q, &f, bad))
+            release_check(b, q, f, k, release_issue(b, q, k), ok, bad);
+    }
+    block_add_counters<2>({ok, bad}, {&b.stats->unpins, &b.stats->bad_unpins});
+}
+
 // One round: release the listed pins, then fetch this round's pages.
 // With one thread this is the deterministic replay of the round.
 // DIST: per-slot hands (b.dist), else the single shared hand.  BYPAGE:
@@ -806,6 +829,15 @@ int launch_round(pbm_bufmgr* m, bool by_page, const int32_t* d_release_of, const
     const int block = serial ? 1 : 256;
     const int grid = serial ? 1 : (int)((work + 255u) / 256u);
     cudaStream_t s = (cudaStream_t)stream;
+    if (n == 0 && !serial) {   // releases only: no fetch, no sweep
+        const int rgrid = (int)((n_release + 255u) / 256u);
+        if (by_page)
+            k_release<true><<<rgrid, 256, 0, s>>>(m->v, d_release_of, d_release_idx, n_release);
+        else
+            k_release<false><<<rgrid, 256, 0, s>>>(m->v, d_release_of, d_release_idx, n_release);
+        PBM_LAUNCH_CHECK();
+        return PBM_OK;
+    }
     auto go = [&](auto kernel) {
         kernel<<<grid, block, 0, s>>>(m->v, d_release_of, d_release_idx, n_release, d_pages, n, slot0, d_frames_out,
                                       d_held_out);

@@ -231,3 +231,35 @@ def test_bad_releases_are_counted_and_undone(cuda, pbm_mod, serial):
     chk = bm.check()
     assert chk.mismatches == 0 and chk.loading == 0 and chk.pins == int(expect.sum())
     bm.close()
+
+
+@pytest.mark.parametrize("by_page", [False, True])
+def test_release_only_round_leaves_the_clock_alone(cuda, pbm_mod, by_page):
+    """A round with releases and no fetches unpins and does nothing else: no
+    sweep runs, so the reference bits (and the frames) stay as they were."""
+    torch = cuda
+    pbm = pbm_mod
+    n_logical, n_frames, R = 1 << 16, 1 << 12, 4096
+    bm = pbm.BufferManager(n_logical, n_frames, policy=0)
+    rng = np.random.default_rng(11)
+    pages = torch.from_numpy(rng.integers(0, n_logical, R).astype(np.int32)).cuda()
+    frames = torch.full((R,), -1, dtype=torch.int32, device="cuda")
+    held = torch.full((R,), -1, dtype=torch.int32, device="cuda")
+    bm.round_pages(None, None, 0, pages, R, 0, frames, held)
+    torch.cuda.synchronize()
+    before = bm.read_tables()
+    assert before[2].sum() > 0                       # fetched pages carry their reference bit
+    idx = torch.arange(R, dtype=torch.int32, device="cuda")
+    if by_page:
+        bm.round_pages(held, idx, R, None, 0, 0, None)
+    else:
+        bm.round(frames, idx, R, None, 0, 0, None)
+    torch.cuda.synchronize()
+    frame, pins, ref, fpage = bm.read_tables()
+    assert np.array_equal(frame, before[0]) and np.array_equal(ref, before[2]) and np.array_equal(fpage, before[3])
+    assert pins.sum() == 0
+    c = bm.counters()
+    assert c.unpins == R and c.bad_unpins == 0
+    chk = bm.check()
+    assert chk.mismatches == 0 and chk.pins == 0
+    bm.close()

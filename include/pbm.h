@@ -376,8 +376,9 @@ int pbm_bufmgr_reset(pbm_bufmgr *m, void *stream);
  * page holds at most 2^30 - 1 pins at a time.  A release of a pin that is not
  * held is counted bad and undone; until it is undone, a fetch of the same
  * page may see it as pinned or, if the page is not resident, wait for it.
- * The lanes of a warp that release the same frame (or page) merge into one
- * release, which is rejected whole if it asks for more pins than are held.
+ * Releases of one frame (or page) in the same block of the launch (in the
+ * same warp for a round of releases only) merge into one release, which is
+ * rejected whole if it asks for more pins than are held.
  * A round with releases and no fetches (n = 0) only unpins: the clock hand
  * and the reference bits stay as they were. */
 int pbm_bufmgr_round(pbm_bufmgr *m, const int32_t *d_frames_of, const int32_t *d_release_idx,

@@ -224,8 +224,9 @@ def test_bad_releases_are_counted_and_undone(cuda, pbm_mod, serial):
         assert c.unpins == 3 and c.bad_unpins == 4
         expect[[5, 6]] = 0
     else:
-        # one warp merges the releases of a name into one atomic: a group
-        # asking for more pins than the page holds is rejected whole
+        # the releases of a name in one warp (one block when the round also
+        # fetches) merge into one atomic: a group asking for more pins than
+        # the page holds is rejected whole
         assert c.unpins == 0 and c.bad_unpins == 7
     assert np.array_equal(pins, expect)
     chk = bm.check()

@@ -1062,7 +1062,8 @@ def run_profile_kernel(args):
     """Small, bounded cases of the other kernels for ncu captures (a few GB
     on the device at most, inputs larger than L2 where the kernel reads
     any): `bufmgr` 16 rounds of 2^18 Zipf fetches on 2^20 frames, full and
-    evicting from round 11 on (k_round),
+    evicting from round 11 on (k_round; --bm-* options set the frames, rounds,
+    hands, releases by page and 4 KiB copies),
     `malloc` 8 rounds of 32 malloc groups + frees on a 2 GiB pool
     (k_malloc_persistent), `alloc` 2^22 collaborative claims at 50%
     (k_alloc_collab) followed by `free` of half of them (k_free_pages)."""
